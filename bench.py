@@ -1,0 +1,394 @@
+"""Benchmark: particle-steps/s of the 2D electrostatic PIC step on one GB300.
+
+Workload (default): two-stream instability on a periodic 2048x2048 grid,
+L = 2 pi, 100 electrons per cell (419,430,400 particles), beams +-0.2 with
+Maxwellian spread 0.01 and a 0.01 sinusoidal perturbation in x, dt = 0.05,
+mixed precision (int32 cell + FP32 offset, FP32 velocity and E, FP64
+charge reduction and diagnostics).  Synthetic inputs from the library's
+seeded init method.  The FP64 plain form runs the same workload for the
+speed-up and the field-energy error.
+
+One JSON line on rank 0.  `value` is device-resident throughput timed with
+CUDA events; `e2e` goes through the C ABI from host buffers (upload,
+pre-step, the steps with a per-step field-energy read-back, download).
+`--impl reference` times the oracle (the CPU restatement of the reference's
+FP64 step) on the host cores instead.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300: FP32-offset vs FP64 plain at ≤1e-5 rel field-energy err"
+UNIT = "particle-steps/s"
+B_P = {"mixed": 40.0, "fp64": 64.0}     # algorithmic bytes per particle-step
+B_G = {"mixed": 40.0, "fp64": 48.0}     # algorithmic bytes per grid node per step
+
+WORKLOADS = {
+    # name: (grid, particles per cell, v0, vth, amp, description)
+    "two_stream_2048": (2048, 100, 0.2, 0.01, 0.01,
+                        "two-stream 2048x2048, 100 electrons/cell (419,430,400), beams +-0.2, "
+                        "vth 0.01, amp 0.01, dt 0.05"),
+    "two_stream_512": (512, 100, 0.2, 0.01, 0.01,
+                       "two-stream 512x512, 100 electrons/cell (26,214,400), beams +-0.2, vth 0.01, "
+                       "amp 0.01, dt 0.05"),
+    "two_stream_64": (64, 100, 0.2, 0.01, 0.01, "two-stream 64x64, 100 electrons/cell (409,600)"),
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def profile_traffic(form):
+    """Per-particle DRAM traffic of the fused particle kernel from the
+    committed ncu summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "k_push_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_particle_%s:" % form):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for p in self.samples:
+            try:
+                sm.append(float(p[0]))
+                mx = float(p[1])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if p[3 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def barrier():
+    ws, _ = dist()
+    if ws > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def max_over_ranks(v):
+    ws, _ = dist()
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([v], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_state(grid, ppc, v0, vth, amp, seed=2024):
+    from cpic_gb300 import _lib
+    n = grid * grid * ppc
+    L = 2 * math.pi
+    x, y, ux, uy = _lib.init_two_stream(seed, 0, n, L, L, v0, vth, amp)
+    q = -L * L / n
+    return dict(n=n, L=L, q=q, m=-q, x=x, y=y, ux=ux, uy=uy)
+
+
+def make_ctx(grid, st, precision, dt):
+    from cpic_gb300 import _lib
+    ctx = _lib.Context(grid, grid, st["L"], st["L"], dt, 1.0, (0.0, 0.0, 0.0), precision=precision,
+                       track_ids=False)
+    return ctx
+
+
+def run_ours(args):
+    from cpic_gb300 import _lib, build
+    build.build()
+    ws, rank = dist()
+    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
+    dt = 0.05
+    st = make_state(grid, ppc, v0, vth, amp, seed=2024 + rank)
+    n = st["n"]
+    ng = grid * grid
+    form = args.precision
+    prec = _lib.MIXED if form == "mixed" else _lib.FP64
+
+    # ---- device-resident throughput (value)
+    ctx = make_ctx(grid, st, prec, dt)
+    ctx.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
+    ctx.pre_step()
+    if args.warmup:
+        ctx.run(args.warmup)
+    barrier()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    t = ctx.time_steps(args.steps)
+    clk = clocks.stop()
+    ms_total = max_over_ranks(t["ms_total"])
+    barrier()
+    we_series = None
+    ms_step = ms_total / args.steps
+    value = ws * n * args.steps / (ms_total / 1e3)
+    push_ms = t["ms_plasma"] / args.steps
+    field_ms = t["ms_field"] / args.steps
+    tile = ctx.tile_info()
+    ctx.close()
+
+    pk, pk_kind = peaks()
+    peak = float(pk.get("hbm_gbs", 6800.0))
+    algo_bytes = B_P[form] * n
+    achieved = algo_bytes / (push_ms / 1e3) / 1e9
+    tpp = profile_traffic(form)
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": pk_kind,
+            "kernel": "k_push (fused gather/push/re-bin/deposit)",
+            "algorithmic_bytes_per_launch": algo_bytes,
+            "traffic": (tpp * n if tpp else None)}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 particle/field math, i32 cells, i64 fixed-point charge, f64 diagnostics"
+           if form == "mixed" else "f64",
+           "data": "synthetic (seeded two-stream init, SplitMix64)",
+           "config": {"workload": desc + (", mixed precision" if form == "mixed" else ", FP64 plain"),
+                      "particles": n, "grid": [grid, grid], "dt": dt, "tile": tile,
+                      "l2": "inputs larger than L2 (particle state %.1f GB)" % (n * 20e-9 if form == "mixed"
+                                                                              else n * 36e-9),
+                      "parallelism": "replicas" if ws > 1 else "single GPU"},
+           "ms_breakdown": {"particle_kernel": push_ms, "field_stage": field_ms},
+           "roofline": roof, "clocks": clk,
+           "gpu_launches": args.steps * (8 if form == "mixed" else 7)}
+
+    # ---- FP64 plain form on the same workload (speed-up and energy error)
+    if form == "mixed" and not args.no_fp64:
+        ctx64 = make_ctx(grid, st, _lib.FP64, dt)
+        ctx64.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
+        ctx64.pre_step()
+        ctxm = make_ctx(grid, st, _lib.MIXED, dt)
+        ctxm.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
+        ctxm.pre_step()
+        worst = 0.0
+        for k in range(args.accuracy_steps):
+            ctx64.step()
+            ctxm.step()
+            a, b = ctxm.field_energy(), ctx64.field_energy()
+            worst = max(worst, abs(a - b) / abs(b))
+        ctxm.close()
+        t64 = ctx64.time_steps(max(2, args.steps // 4))
+        ms64 = t64["ms_total"] / max(2, args.steps // 4)
+        ctx64.close()
+        v64 = ws * n / (ms64 / 1e3)
+        out["fp64_plain"] = {"value": v64, "ms_per_step": ms64,
+                             "particle_kernel_ms": t64["ms_plasma"] / max(2, args.steps // 4)}
+        out["speedup_vs_fp64"] = value / v64
+        out["we_rel_err_vs_fp64"] = {"steps": args.accuracy_steps, "max": worst}
+
+    # ---- end to end through the C ABI with host buffers
+    if not args.no_e2e:
+        e2e_steps = max(args.steps, args.e2e_steps)
+        from cpic_gb300 import _lib as L
+        host = {k: st[k] for k in ("x", "y", "ux", "uy")}
+        outx = [np.empty(n) for _ in range(4)]
+        barrier()
+        t0 = time.perf_counter()
+        ctx = make_ctx(grid, st, prec, dt)
+        ctx.add_species(st["q"], st["m"], host["x"], host["y"], host["ux"], host["uy"])
+        ctx.pre_step()
+        for k in range(e2e_steps):
+            ctx.run(1)
+            we = ctx.field_energy()
+        ctx.lib.cpic_get_particles(ctx.h, 0, *[L._dp(a) for a in outx])
+        t1 = time.perf_counter()
+        ctx.close()
+        el = max_over_ranks(t1 - t0)
+        out["e2e"] = {"value": ws * n * e2e_steps / el, "unit": UNIT, "steps": e2e_steps,
+                      "seconds": el,
+                      "h2d_bytes_per_step": 4 * 8 * n / e2e_steps,
+                      "d2h_bytes_per_step": 4 * 8 * n / e2e_steps + 5 * 8,
+                      "path": "cpic_create/cpic_add_species/cpic_pre_step, per step cpic_run(1) + "
+                              "cpic_field_energy read-back, cpic_get_particles"}
+
+    # ---- CPU baseline: the oracle on a bounded sample of the workload
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(grid, ppc, v0, vth, amp, dt, n, threads=1)
+    return out
+
+
+def _oracle_sample(grid, ppc, v0, vth, amp, dt, frac, seed):
+    """Time the oracle on the full grid with a fraction of the particles;
+    returns (seconds per particle-step, seconds per field solve)."""
+    from oracle.oracle import Oracle
+    from cpic_gb300 import _lib
+    n = max(1024, int(grid * grid * ppc * frac))
+    L = 2 * math.pi
+    x, y, ux, uy = _lib.init_two_stream(seed, 0, n, L, L, v0, vth, amp)
+    q = -L * L / n
+    o = Oracle(grid, grid, L, L, dt, 1.0, (0.0, 0.0, 0.0))
+    o.add_species(q, -q, x, y, ux, uy)
+    o.pre_step()
+    o.step()
+    tf = tp = 0.0
+    steps = 2
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.stage_field_E()
+        t1 = time.perf_counter()
+        o.stage_plasma_E()
+        o.stage_plasma_r()
+        o.stage_field_rho()
+        o.iter = o.iter + 1
+        t2 = time.perf_counter()
+        tf += t1 - t0
+        tp += t2 - t1
+    o.close()
+    return tp / (n * steps), tf / steps, n, steps
+
+
+def cpu_baseline(grid, ppc, v0, vth, amp, dt, n_full, threads=1):
+    frac = 1.0 / 16 if grid >= 1024 else 1.0
+    if threads <= 1:
+        cp, cg, ns, steps = _oracle_sample(grid, ppc, v0, vth, amp, dt, frac, 99)
+        per_step = n_full * cp + cg
+        return {"value": n_full / per_step, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": "oracle (FP64 C restatement of the reference step) on the full %dx%d grid "
+                          "with %d particles (1/%d of the workload), %d timed steps; particle cost "
+                          "%.1f ns/particle-step and field solve %.3f s/step scaled to %d particles"
+                          % (grid, grid, ns, round(1 / frac), steps, cp * 1e9, cg, n_full)}
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(threads) as pool:
+        res = pool.starmap(_oracle_sample, [(grid, ppc, v0, vth, amp, dt, frac, 99 + i)
+                                            for i in range(threads)])
+    cp = statistics.mean(r[0] for r in res)
+    cg = statistics.mean(r[1] for r in res)
+    ns, steps = res[0][2], res[0][3]
+    per_step = n_full * cp + cg
+    # independent replicas on every core: aggregate throughput
+    return {"value": threads * n_full / per_step, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d concurrent oracle processes (FP64 C restatement of the reference step), each "
+                      "on the full %dx%d grid with %d particles (1/%d of the workload), %d timed "
+                      "steps; per-process cost %.1f ns/particle-step + %.3f s field solve per step, "
+                      "scaled to %d particles per replica"
+                      % (threads, grid, grid, ns, round(1 / frac), steps, cp * 1e9, cg, n_full)}
+
+
+def run_reference(args):
+    ws, rank = dist()
+    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
+    if rank != 0:
+        return None
+    from cpic_gb300 import build
+    build.build()
+    from oracle import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cb = cpu_baseline(grid, ppc, v0, vth, amp, 0.05, grid * grid * ppc, threads=threads)
+    el = time.perf_counter() - t0
+    v = cb["value"]
+    return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": grid * grid * ppc / v * 1e3 / threads,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded two-stream init, SplitMix64)",
+            "config": {"workload": desc + ", FP64 (reference algorithm on host cores)",
+                       "particles": grid * grid * ppc, "grid": [grid, grid], "dt": 0.05},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"] + "; the reference itself needs MPI, FFTW and "
+                             "libconfig, which are not on the host, so its restatement runs"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_seconds": el}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="two_stream_2048", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--accuracy-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 0)
+    ws, rank = dist()
+    if ws > 1:
+        import torch
+        import torch.distributed as td
+        td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1316 @@
+// cpic_ctx.cu -- host context and C ABI (include/cpic_gpu.h), plus the
+// generic device kernels: tile fix-up, counting-sort rebuild of the
+// particle store, host views and FP64 diagnostics.
+//
+// Compiled with --fmad=false: the tile of an FP64 particle computed here
+// must agree bit for bit with the one the push kernel computes.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/cpic_gpu.h"
+#include "cpic_common.cuh"
+#include "cpic_push.cuh"
+
+namespace cpic {
+void launch_gather_f64_tiles(const Grid &g, const StoreF64 &st, const int64_t *base,
+		const int32_t *cnt, int ntiles, const double *Ex, const double *Ey,
+		double *ex_out, double *ey_out, cudaStream_t s);
+void launch_gather_mix_tiles(const Grid &g, const StoreMix &st, const int64_t *base,
+		const int32_t *cnt, int ntiles, const float2 *E, double *ex_out, double *ey_out,
+		cudaStream_t s);
+}
+
+using namespace cpic;
+
+#define CK(call) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) { \
+	fprintf(stderr, "cpic: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_), \
+		__FILE__, __LINE__); return CPIC_ECUDA; } } while(0)
+
+// ------------------------------------------------------------- context
+
+struct SpeciesHost {
+	double q, m;
+	int64_t n;
+	int64_t cap_main, cap_alt;  // slots allocated in the store and its alternate
+	StoreF64 f64, f64_alt;
+	StoreMix mix, mix_alt;
+	Tiles tiles;
+	Spill spill[2];          // ping-pong: spill[cur] is the input
+	double vmax;              // largest initial |u| component
+};
+
+struct cpic_ctx {
+	cpic_params_t p;
+	Grid g;
+	int ntiles;
+	int precision;
+	int64_t iter;
+	bool prepared;
+	double qscale, qinv;
+	cudaStream_t stream;
+	int nspecies;
+	SpeciesHost sp[kMaxSpecies];
+	int spill_cur;
+	// fields
+	long long *rho;           // ny x nx fixed point
+	double *phi64, *Ex64, *Ey64;
+	float *phi32;
+	float2 *E32;
+	double2 *spec64;
+	float2 *spec32;
+	double2 *twx64, *twy64;
+	float2 *twx32, *twy32;
+	double *cosx, *cosy;
+	double *mean;             // device scalar (mixed form)
+	long long *rho_sum;       // device scalar
+	uint32_t *status;
+	double *scratch;          // FP64 scratch for host views / partial sums
+	size_t scratch_n;
+	int32_t *counter;         // device scalar
+};
+
+// ------------------------------------------------------------- kernels
+
+// Closes the gap between the compacted stayers and the appended movers.
+template <class F>
+__global__ void k_fixup(const PushArgs a)
+{
+	int s = blockIdx.y, t = blockIdx.x;
+	const Tiles &T = a.tiles[s];
+	int cnt_old = T.cnt[t], stay = T.stay[t];
+	int app = min(T.app[t], T.cap[t]);
+	int inc = app - cnt_old;
+	int gap = cnt_old - stay;
+	int k = min(gap, inc);
+	int64_t b = T.base[t];
+	for(int i = threadIdx.x; i < k; i += blockDim.x)
+	{
+		typename F::Rec r = F::load(a, s, b + app - k + i);
+		F::store(a, s, b + stay + i, r);
+	}
+	if(threadIdx.x == 0)
+	{
+		T.cnt[t] = stay + inc;
+		T.app[t] = stay + inc;
+	}
+}
+
+// Tile of a record given in the FP64 spill layout.
+template <class F> struct TileOf;
+template <> struct TileOf<F64> {
+	static __device__ __forceinline__ int get(const Grid &g, const Spill &S, int64_t k)
+	{
+		double w[4];
+		int cx, cy;
+		F64::weights(g, S.x[k], S.y[k], w, cx, cy);
+		cx = min(max(cx, 0), g.nx - 1);
+		cy = min(max(cy, 0), g.ny - 1);
+		return tile_of(g, cx, cy);
+	}
+};
+template <> struct TileOf<Mix> {
+	static __device__ __forceinline__ int get(const Grid &g, const Spill &S, int64_t k)
+	{
+		Mix::Rec r = Mix::from_spill(S, k, g);
+		return tile_of(g, r.cell % g.nx, r.cell / g.nx);
+	}
+};
+
+template <class F>
+__global__ void k_rb_count(Grid g, Spill S, int64_t n, int32_t *newcnt)
+{
+	for(int64_t k = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; k < n;
+			k += (int64_t) gridDim.x * blockDim.x)
+		atomicAdd(&newcnt[TileOf<F>::get(g, S, k)], 1);
+}
+
+// Copy each tile's particles from the old store to the new base.
+template <class F>
+__global__ void k_rb_copy(const PushArgs olda, const PushArgs newa, int s)
+{
+	int t = blockIdx.x;
+	int n = olda.tiles[s].cnt[t];
+	int64_t ob = olda.tiles[s].base[t], nb = newa.tiles[s].base[t];
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		typename F::Rec r = F::load(olda, s, ob + i);
+		F::store(newa, s, nb + i, r);
+	}
+}
+
+template <class F>
+__global__ void k_rb_scatter(const PushArgs newa, int s, Spill S, int64_t n, int32_t *fill)
+{
+	const Grid &g = newa.g;
+	for(int64_t k = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; k < n;
+			k += (int64_t) gridDim.x * blockDim.x)
+	{
+		int t = TileOf<F>::get(g, S, k);
+		int slot = atomicAdd(&fill[t], 1);
+		typename F::Rec r = F::from_spill(S, k, g);
+		F::store(newa, s, newa.tiles[s].base[t] + slot, r);
+	}
+}
+
+// Host view: FP64 state by particle id (or compacted through a counter).
+template <class F>
+__global__ void k_download(const PushArgs a, int s, double *x, double *y, double *ux,
+		double *uy, int32_t *counter, int by_id)
+{
+	int t = blockIdx.x;
+	int n = a.tiles[s].cnt[t];
+	int64_t b = a.tiles[s].base[t];
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		typename F::Rec r = F::load(a, s, b + i);
+		double px, py, pu, pv;
+		F::to_spill_vals(r, a.g, px, py, pu, pv);
+		int64_t dst = by_id ? r.id : atomicAdd(counter, 1);
+		x[dst] = px; y[dst] = py; ux[dst] = pu; uy[dst] = pv;
+	}
+}
+
+template <class F>
+__global__ void k_cell_counts(const PushArgs a, int s, unsigned long long *counts)
+{
+	int t = blockIdx.x;
+	int n = a.tiles[s].cnt[t];
+	int64_t b = a.tiles[s].base[t];
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		typename F::Rec r = F::load(a, s, b + i);
+		int cx, cy;
+		F::cell_of(r, a.g, cx, cy);
+		if(cx >= 0 && cx < a.g.nx && cy >= 0 && cy < a.g.ny)
+			atomicAdd(&counts[(int64_t) cy * a.g.nx + cx], 1ULL);
+	}
+}
+
+// Per-tile partial sums of m|u|^2 and m u (FP64), deterministic per tile.
+template <class F>
+__global__ void k_kinetic(const PushArgs a, int s, double m, double *part)
+{
+	__shared__ double sh[3][256];
+	int t = blockIdx.x;
+	int n = a.tiles[s].cnt[t];
+	int64_t b = a.tiles[s].base[t];
+	double k = 0.0, px = 0.0, py = 0.0;
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		typename F::Rec r = F::load(a, s, b + i);
+		double x, y, u, v;
+		F::to_spill_vals(r, a.g, x, y, u, v);
+		k += u * u + v * v;
+		px += u;
+		py += v;
+	}
+	sh[0][threadIdx.x] = k; sh[1][threadIdx.x] = px; sh[2][threadIdx.x] = py;
+	__syncthreads();
+	for(int st = 128; st > 0; st >>= 1)
+	{
+		if(threadIdx.x < st)
+			for(int c = 0; c < 3; c++)
+				sh[c][threadIdx.x] += sh[c][threadIdx.x + st];
+		__syncthreads();
+	}
+	if(threadIdx.x == 0)
+	{
+		part[3 * t + 0] = 0.5 * m * sh[0][0];
+		part[3 * t + 1] = m * sh[1][0];
+		part[3 * t + 2] = m * sh[2][0];
+	}
+}
+
+// Field energy partial sums over rows (one block per row), FP64.
+__global__ void k_field_energy(Grid g, const double *Ex, const double *Ey, const float2 *E32,
+		const long long *rho, double *part)
+{
+	__shared__ double sh[2][256];
+	int iy = blockIdx.x;
+	double e = 0.0;
+	long long q = 0;
+	for(int ix = threadIdx.x; ix < g.nx; ix += blockDim.x)
+	{
+		int64_t i = (int64_t) iy * g.nx + ix;
+		double ex, ey;
+		if(E32) { ex = E32[i].x; ey = E32[i].y; }
+		else { ex = Ex[i]; ey = Ey[i]; }
+		e += ex * ex + ey * ey;
+		q += rho[i];
+	}
+	sh[0][threadIdx.x] = e;
+	sh[1][threadIdx.x] = (double) 0;
+	__shared__ long long shq[256];
+	shq[threadIdx.x] = q;
+	__syncthreads();
+	for(int st = 128; st > 0; st >>= 1)
+	{
+		if(threadIdx.x < st)
+		{
+			sh[0][threadIdx.x] += sh[0][threadIdx.x + st];
+			shq[threadIdx.x] += shq[threadIdx.x + st];
+		}
+		__syncthreads();
+	}
+	if(threadIdx.x == 0)
+	{
+		part[2 * iy] = sh[0][0];
+		part[2 * iy + 1] = (double) shq[0];
+	}
+}
+
+// Exact int64 sum of rho, then the mean as FP64 (mixed form k=0 removal).
+__global__ void k_rho_mean(int64_t n, const long long *rho, long long *sum, double qinv,
+		double *mean)
+{
+	__shared__ long long sh[1024];
+	long long v = 0;
+	for(int64_t i = threadIdx.x; i < n; i += blockDim.x)
+		v += rho[i];
+	sh[threadIdx.x] = v;
+	__syncthreads();
+	for(int st = blockDim.x / 2; st > 0; st >>= 1)
+	{
+		if(threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+		__syncthreads();
+	}
+	if(threadIdx.x == 0)
+	{
+		*sum = sh[0];
+		*mean = (double) sh[0] * qinv / (double) n;
+	}
+}
+
+__global__ void k_rho_to_f64(int64_t n, const long long *rho, double qinv, double *out)
+{
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+			i += (int64_t) gridDim.x * blockDim.x)
+		out[i] = (double) rho[i] * qinv;
+}
+
+__global__ void k_f64_to_rho(int64_t n, const double *in, double qscale, long long *rho)
+{
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+			i += (int64_t) gridDim.x * blockDim.x)
+		rho[i] = __double2ll_rn(in[i] * qscale);
+}
+
+__global__ void k_iota(int64_t n, int32_t *id)
+{
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+			i += (int64_t) gridDim.x * blockDim.x)
+		id[i] = (int32_t) i;
+}
+
+// Y wrap of the initial global exchange (sim_pre_step -> comm_plasma(sim,
+// 1), src/comm_plasma.c:1087-1112): one periodic wrap in Y.
+__global__ void k_wrap_y(int64_t n, double *y, double Ly)
+{
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+			i += (int64_t) gridDim.x * blockDim.x)
+	{
+		double v = y[i];
+		if(v >= Ly) v -= Ly;
+		else if(v < 0.0) v += Ly;
+		y[i] = v;
+	}
+}
+
+// ------------------------------------------------------------- helpers
+
+static int grid_blocks(int64_t n, int threads = 256, int maxb = 4096)
+{
+	int64_t b = (n + threads - 1) / threads;
+	if(b < 1) b = 1;
+	if(b > maxb) b = maxb;
+	return (int) b;
+}
+
+static int ilog2(int64_t v)
+{
+	int l = 0;
+	while(((int64_t) 1 << l) < v) l++;
+	return l;
+}
+
+static bool pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+
+static PushArgs make_args(cpic_ctx *c, int cur_spill)
+{
+	PushArgs a;
+	memset(&a, 0, sizeof(a));
+	a.g = c->g;
+	a.nspecies = c->nspecies;
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		a.tiles[s] = c->sp[s].tiles;
+		a.f64[s] = c->sp[s].f64;
+		a.mix[s] = c->sp[s].mix;
+		a.spill_out[s] = c->sp[s].spill[cur_spill ^ 1];
+	}
+	a.rho = c->rho;
+	a.Ex64 = c->Ex64;
+	a.Ey64 = c->Ey64;
+	a.E32 = c->precision == CPIC_MIXED ? c->E32 : nullptr;
+	a.status = c->status;
+	return a;
+}
+
+static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
+{
+	const cpic_params_t &p = c->p;
+	double dt = iter == 0 ? -p.dt / 2 : p.dt;
+	a.iter = (int) (iter == 0 ? 0 : 1);
+	a.dt = dt;
+	a.cdx_f = (float) (p.dt / c->g.dx);
+	a.cdy_f = (float) (p.dt / c->g.dy);
+	int64_t chunks = p.plasma_chunks > 0 ? p.plasma_chunks : 1;
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		SpeciesStep &st = a.sp[s];
+		double q = c->sp[s].q, m = c->sp[s].m;
+		// chunk_update_r, mover.c:204-225
+		st.dtqm2 = 0.5 * dt * q / m;
+		// boris_rotation, mover.c:43-51
+		st.tz = p.B[2] * st.dtqm2;
+		double sd = 1.0;
+		sd += st.tz * st.tz;
+		st.sz = 2.0 * st.tz / sd;
+		// umax, sim.c:198-200
+		st.umax_x = (c->g.nx / chunks) * c->g.dx / p.dt;
+		st.umax_y = c->g.ny * c->g.dy / p.dt;
+		double vq = -q / p.e0;
+		st.qfix = vq * c->qscale;
+		st.qfix_f = (float) st.qfix;
+		st.dtqm2_f = (float) st.dtqm2;
+		st.tz_f = (float) st.tz;
+		st.sz_f = (float) st.sz;
+	}
+}
+
+static size_t push_smem(const cpic_ctx *c)
+{
+	int W = c->g.tx + 2 * c->g.halo + 1;
+	size_t sm = (size_t) W * W * sizeof(long long);
+	if(c->precision == CPIC_MIXED)
+		sm += (size_t) (c->g.tx + 1) * (c->g.ty + 1) * sizeof(float2);
+	return sm;
+}
+
+static int check_status(cpic_ctx *c)
+{
+	uint32_t st = 0;
+	CK(cudaStreamSynchronize(c->stream));
+	CK(cudaMemcpy(&st, c->status, sizeof(st), cudaMemcpyDeviceToHost));
+	if(st & ST_SPILL_FULL) return CPIC_ECAPACITY;
+	if(st & ST_UMAX) return CPIC_EUMAX;
+	if(st & ST_NAN) return CPIC_ENAN;
+	if(st & ST_RANGE) return CPIC_EINVAL;
+	return CPIC_OK;
+}
+
+static int alloc_store(cpic_ctx *c, SpeciesHost &S, int64_t cap, bool alt)
+{
+	if(c->precision == CPIC_FP64)
+	{
+		StoreF64 &st = alt ? S.f64_alt : S.f64;
+		CK(cudaMalloc(&st.x, cap * sizeof(double)));
+		CK(cudaMalloc(&st.y, cap * sizeof(double)));
+		CK(cudaMalloc(&st.ux, cap * sizeof(double)));
+		CK(cudaMalloc(&st.uy, cap * sizeof(double)));
+		CK(cudaMalloc(&st.id, cap * sizeof(int32_t)));
+	}
+	else
+	{
+		StoreMix &st = alt ? S.mix_alt : S.mix;
+		CK(cudaMalloc(&st.cell, cap * sizeof(int32_t)));
+		CK(cudaMalloc(&st.ox, cap * sizeof(float)));
+		CK(cudaMalloc(&st.oy, cap * sizeof(float)));
+		CK(cudaMalloc(&st.ux, cap * sizeof(float)));
+		CK(cudaMalloc(&st.uy, cap * sizeof(float)));
+		st.id = nullptr;
+		if(c->p.track_ids)
+			CK(cudaMalloc(&st.id, cap * sizeof(int32_t)));
+	}
+	return CPIC_OK;
+}
+
+static void free_store(cpic_ctx *c, SpeciesHost &S, bool alt)
+{
+	if(c->precision == CPIC_FP64)
+	{
+		StoreF64 &st = alt ? S.f64_alt : S.f64;
+		cudaFree(st.x); cudaFree(st.y); cudaFree(st.ux); cudaFree(st.uy); cudaFree(st.id);
+		memset(&st, 0, sizeof(st));
+	}
+	else
+	{
+		StoreMix &st = alt ? S.mix_alt : S.mix;
+		cudaFree(st.cell); cudaFree(st.ox); cudaFree(st.oy); cudaFree(st.ux); cudaFree(st.uy);
+		cudaFree(st.id);
+		memset(&st, 0, sizeof(st));
+	}
+}
+
+static int alloc_spill(Spill &S, int32_t capacity)
+{
+	S.capacity = capacity;
+	CK(cudaMalloc(&S.x, (size_t) capacity * sizeof(double)));
+	CK(cudaMalloc(&S.y, (size_t) capacity * sizeof(double)));
+	CK(cudaMalloc(&S.ux, (size_t) capacity * sizeof(double)));
+	CK(cudaMalloc(&S.uy, (size_t) capacity * sizeof(double)));
+	CK(cudaMalloc(&S.id, (size_t) capacity * sizeof(int32_t)));
+	CK(cudaMalloc(&S.count, sizeof(int32_t)));
+	CK(cudaMemset(S.count, 0, sizeof(int32_t)));
+	return CPIC_OK;
+}
+
+static void free_spill(Spill &S)
+{
+	cudaFree(S.x); cudaFree(S.y); cudaFree(S.ux); cudaFree(S.uy); cudaFree(S.id);
+	cudaFree(S.count);
+	memset(&S, 0, sizeof(S));
+}
+
+template <class F>
+static void launch_rb_copy(const PushArgs &o, const PushArgs &n, int s, int nt, cudaStream_t st)
+{
+	k_rb_copy<F><<<nt, 256, 0, st>>>(o, n, s);
+}
+
+template <class F>
+static void launch_rb_scatter(const PushArgs &n, int s, const Spill &S, int64_t cnt,
+		int32_t *fill, cudaStream_t st)
+{
+	if(cnt > 0)
+		k_rb_scatter<F><<<grid_blocks(cnt), 256, 0, st>>>(n, s, S, cnt, fill);
+}
+
+template <class F>
+static void launch_rb_count(const Grid &g, const Spill &S, int64_t cnt, int32_t *newcnt,
+		cudaStream_t st)
+{
+	if(cnt > 0)
+		k_rb_count<F><<<grid_blocks(cnt), 256, 0, st>>>(g, S, cnt, newcnt);
+}
+
+// Counting-sort rebuild of species s: its tiles (unless `fresh`), its
+// current spill input and an optional staging list are merged into a new
+// layout whose tile capacities follow the new counts.
+static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging, int64_t nstage)
+{
+	SpeciesHost &S = c->sp[s];
+	int nt = c->ntiles;
+	cudaStream_t st = c->stream;
+	Spill &spin = S.spill[c->spill_cur];
+	int32_t nspill = 0;
+	CK(cudaMemcpyAsync(&nspill, spin.count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	if(nspill > spin.capacity) nspill = spin.capacity;
+
+	int32_t *newcnt = nullptr, *fill = nullptr;
+	CK(cudaMalloc(&newcnt, nt * sizeof(int32_t)));
+	CK(cudaMalloc(&fill, nt * sizeof(int32_t)));
+	if(fresh)
+		CK(cudaMemsetAsync(newcnt, 0, nt * sizeof(int32_t), st));
+	else
+		CK(cudaMemcpyAsync(newcnt, S.tiles.cnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+	bool mix = c->precision == CPIC_MIXED;
+	if(mix)
+	{
+		launch_rb_count<Mix>(c->g, spin, nspill, newcnt, st);
+		if(staging) launch_rb_count<Mix>(c->g, *staging, nstage, newcnt, st);
+	}
+	else
+	{
+		launch_rb_count<F64>(c->g, spin, nspill, newcnt, st);
+		if(staging) launch_rb_count<F64>(c->g, *staging, nstage, newcnt, st);
+	}
+	std::vector<int32_t> hc(nt);
+	CK(cudaMemcpyAsync(hc.data(), newcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+
+	// capacities: 25% slack plus 64 slots, rounded to 32
+	std::vector<int64_t> hb(nt);
+	std::vector<int32_t> hcap(nt);
+	int64_t total = 0, n = 0;
+	for(int t = 0; t < nt; t++)
+	{
+		int64_t cap = hc[t] + hc[t] / 4 + 64;
+		cap = (cap + 31) & ~(int64_t) 31;
+		if(cap > INT32_MAX) return CPIC_ECAPACITY;
+		hb[t] = total;
+		hcap[t] = (int32_t) cap;
+		total += cap;
+		n += hc[t];
+	}
+
+	// the alternate store receives the new layout
+	bool have_alt = mix ? S.mix_alt.ux != nullptr : S.f64_alt.ux != nullptr;
+	if(S.cap_alt < total || !have_alt)
+	{
+		free_store(c, S, true);
+		int r = alloc_store(c, S, total, true);
+		if(r) return r;
+		S.cap_alt = total;
+	}
+	int64_t *nbase;
+	int32_t *ncap;
+	CK(cudaMalloc(&nbase, nt * sizeof(int64_t)));
+	CK(cudaMalloc(&ncap, nt * sizeof(int32_t)));
+	CK(cudaMemcpyAsync(nbase, hb.data(), nt * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(ncap, hcap.data(), nt * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+
+	PushArgs olda = make_args(c, c->spill_cur);
+	PushArgs newa = olda;
+	newa.tiles[s].base = nbase;
+	newa.tiles[s].cap = ncap;
+	newa.f64[s] = S.f64_alt;
+	newa.mix[s] = S.mix_alt;
+	if(fresh)
+		CK(cudaMemsetAsync(fill, 0, nt * sizeof(int32_t), st));
+	else
+		CK(cudaMemcpyAsync(fill, S.tiles.cnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+	if(!fresh)
+	{
+		if(mix) launch_rb_copy<Mix>(olda, newa, s, nt, st);
+		else launch_rb_copy<F64>(olda, newa, s, nt, st);
+	}
+	if(mix)
+	{
+		launch_rb_scatter<Mix>(newa, s, spin, nspill, fill, st);
+		if(staging) launch_rb_scatter<Mix>(newa, s, *staging, nstage, fill, st);
+	}
+	else
+	{
+		launch_rb_scatter<F64>(newa, s, spin, nspill, fill, st);
+		if(staging) launch_rb_scatter<F64>(newa, s, *staging, nstage, fill, st);
+	}
+	CK(cudaGetLastError());
+	CK(cudaMemsetAsync(spin.count, 0, sizeof(int32_t), st));
+	CK(cudaMemcpyAsync(S.tiles.cnt, newcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+	CK(cudaMemcpyAsync(S.tiles.app, newcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+	CK(cudaMemcpyAsync(S.tiles.base, nbase, nt * sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
+	CK(cudaMemcpyAsync(S.tiles.cap, ncap, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+	CK(cudaStreamSynchronize(st));
+	cudaFree(nbase); cudaFree(ncap); cudaFree(newcnt); cudaFree(fill);
+	// swap stores; the old one becomes the alternate
+	std::swap(S.f64, S.f64_alt);
+	std::swap(S.mix, S.mix_alt);
+	std::swap(S.cap_main, S.cap_alt);
+	S.n = n;
+	return CPIC_OK;
+}
+
+static int rebuild_if_spilled(cpic_ctx *c)
+{
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		int32_t ns = 0;
+		CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
+				cudaMemcpyDeviceToHost));
+		if(ns > 0)
+		{
+			int r = rebuild_species(c, s, false, nullptr, 0);
+			if(r) return r;
+		}
+	}
+	return CPIC_OK;
+}
+
+// One fused particle stage (gather, push, re-bin, deposit) without
+// host synchronisation.  deposit_only: the initial charge deposit.
+static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = nullptr,
+		cudaEvent_t ev1 = nullptr)
+{
+	cudaStream_t st = c->stream;
+	int64_t ng = (int64_t) c->g.nx * c->g.ny;
+	CK(cudaMemsetAsync(c->rho, 0, ng * sizeof(long long), st));
+	int cur = c->spill_cur;
+	for(int s = 0; s < c->nspecies; s++)
+		CK(cudaMemsetAsync(c->sp[s].spill[cur ^ 1].count, 0, sizeof(int32_t), st));
+	SpillArgs sa;
+	memset(&sa, 0, sizeof(sa));
+	sa.p = make_args(c, cur);
+	fill_species_step(c, sa.p, deposit_only ? 0 : c->iter);
+	if(deposit_only)
+	{
+		// no field, no push: deposit the current positions (pre-step)
+		for(int s = 0; s < c->nspecies; s++)
+		{
+			sa.p.sp[s].dtqm2 = 0.0; sa.p.sp[s].tz = 0.0; sa.p.sp[s].sz = 0.0;
+			sa.p.sp[s].dtqm2_f = 0.0f; sa.p.sp[s].tz_f = 0.0f; sa.p.sp[s].sz_f = 0.0f;
+			sa.p.sp[s].umax_x = INFINITY; sa.p.sp[s].umax_y = INFINITY;
+		}
+		sa.p.iter = 0;
+	}
+	for(int s = 0; s < c->nspecies; s++)
+		sa.spill_in[s] = c->sp[s].spill[cur];
+	size_t smem = push_smem(c);
+	if(ev0) CK(cudaEventRecord(ev0, st));
+	if(c->precision == CPIC_MIXED)
+		launch_push_mix(sa.p, c->ntiles, smem, st);
+	else
+		launch_push_f64(sa.p, c->ntiles, smem, st);
+	if(ev1) CK(cudaEventRecord(ev1, st));
+	CK(cudaGetLastError());
+	if(c->precision == CPIC_MIXED)
+		launch_spill_mix(sa, st);
+	else
+		launch_spill_f64(sa, st);
+	dim3 fg(c->ntiles, c->nspecies);
+	if(c->precision == CPIC_MIXED)
+		k_fixup<Mix><<<fg, 256, 0, st>>>(sa.p);
+	else
+		k_fixup<F64><<<fg, 256, 0, st>>>(sa.p);
+	CK(cudaGetLastError());
+	c->spill_cur ^= 1;
+	return CPIC_OK;
+}
+
+static int field_stage_async(cpic_ctx *c)
+{
+	cudaStream_t st = c->stream;
+	if(c->precision == CPIC_MIXED)
+	{
+		int64_t ng = (int64_t) c->g.nx * c->g.ny;
+		k_rho_mean<<<1, 1024, 0, st>>>(ng, c->rho, c->rho_sum, c->qinv, c->mean);
+		launch_poisson_mix(c->g, c->rho, c->qinv, c->mean, c->spec32, c->twx32, c->twy32,
+				c->cosx, c->cosy, c->phi32, st);
+		launch_E_mix(c->g, c->phi32, c->E32, st);
+	}
+	else
+	{
+		launch_poisson_f64(c->g, c->rho, c->qinv, nullptr, c->spec64, c->twx64, c->twy64,
+				c->cosx, c->cosy, c->phi64, st);
+		launch_E_f64(c->g, c->phi64, c->Ex64, c->Ey64, st);
+	}
+	CK(cudaGetLastError());
+	return CPIC_OK;
+}
+
+static int ensure_scratch(cpic_ctx *c, size_t n)
+{
+	if(c->scratch_n >= n) return CPIC_OK;
+	cudaFree(c->scratch);
+	c->scratch = nullptr;
+	CK(cudaMalloc(&c->scratch, n * sizeof(double)));
+	c->scratch_n = n;
+	return CPIC_OK;
+}
+
+// ------------------------------------------------------------- C ABI
+
+extern "C" {
+
+CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
+{
+	if(!p || !out) return CPIC_EINVAL;
+	*out = nullptr;
+	if(!pow2(p->nx) || !pow2(p->ny) || p->nx < 4 || p->ny < 4 || p->nx > (1 << 14)
+			|| p->ny > (1 << 14))
+		return CPIC_EINVAL;
+	if(!(p->Lx > 0) || !(p->Ly > 0) || !(p->dt > 0) || !(p->e0 > 0))
+		return CPIC_EINVAL;
+	// The reference rejects any non-zero u_z (umax[Z] = 0, mover.c:97-137,
+	// sim.c:200), which an in-plane B would produce on the first step.
+	if(p->B[0] != 0.0 || p->B[1] != 0.0)
+		return CPIC_EINVAL;
+	if(p->precision != CPIC_FP64 && p->precision != CPIC_MIXED)
+		return CPIC_EINVAL;
+	int ndev = 0;
+	if(cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+		return CPIC_ENODEV;
+
+	cpic_ctx *c = new cpic_ctx();
+	memset((void *) c, 0, sizeof(*c));
+	c->p = *p;
+	c->precision = p->precision;
+	c->iter = -1;
+	Grid &g = c->g;
+	g.nx = (int) p->nx; g.ny = (int) p->ny;
+	g.Lx = p->Lx; g.Ly = p->Ly;
+	// sim_prepare, sim.c:171-175
+	g.dx = p->Lx / p->nx;
+	g.dy = p->Ly / p->ny;
+	// interpolate_f2p_E / interpolate_p2f_rho, interpolate.c:303-304
+	g.idx = 1.0 / g.dx;
+	g.idy = 1.0 / g.dy;
+	int T = p->tile_x;
+	if(T <= 0)
+	{
+		// autotune default: the largest tile with at least 2048 tiles,
+		// else the largest tile giving at least 64 tiles, else 4 cells
+		T = 4;
+		for(int cand = 64; cand >= 4; cand >>= 1)
+			if(p->nx % cand == 0 && p->ny % cand == 0
+					&& (p->nx / cand) * (p->ny / cand) >= 2048) { T = cand; break; }
+		if(T == 4)
+			for(int cand = 32; cand >= 4; cand >>= 1)
+				if(p->nx % cand == 0 && p->ny % cand == 0
+						&& (p->nx / cand) * (p->ny / cand) >= 64) { T = cand; break; }
+	}
+	int TY = p->tile_y > 0 ? p->tile_y : T;
+	if(!pow2(T) || !pow2(TY) || p->nx % T || p->ny % TY || T != TY)
+	{
+		delete c;
+		return CPIC_EINVAL;
+	}
+	g.tx = T; g.ty = TY;
+	g.ntx = g.nx / T; g.nty = g.ny / TY;
+	g.halo = p->halo > 0 ? p->halo : 2;
+	c->ntiles = g.ntx * g.nty;
+	if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+	{
+		delete c;
+		return CPIC_ECUDA;
+	}
+	int64_t ng = (int64_t) g.nx * g.ny;
+	int64_t nh = g.nx / 2 + 1;
+	int r = CPIC_OK;
+#define AL(ptr, bytes) do { if(cudaMalloc(&(ptr), (bytes)) != cudaSuccess) { r = CPIC_ENOMEM; goto fail; } } while(0)
+	AL(c->rho, ng * sizeof(long long));
+	AL(c->status, sizeof(uint32_t));
+	AL(c->cosx, g.nx * sizeof(double));
+	AL(c->cosy, g.ny * sizeof(double));
+	AL(c->mean, sizeof(double));
+	AL(c->rho_sum, sizeof(long long));
+	AL(c->counter, sizeof(int32_t));
+	if(c->precision == CPIC_FP64)
+	{
+		AL(c->phi64, ng * sizeof(double));
+		AL(c->Ex64, (ng + 3 * (int64_t) g.nx) * sizeof(double));
+		AL(c->Ey64, (ng + 3 * (int64_t) g.nx) * sizeof(double));
+		AL(c->spec64, ng / g.nx * nh * sizeof(double2));
+		AL(c->twx64, g.nx / 2 * sizeof(double2));
+		AL(c->twy64, g.ny / 2 * sizeof(double2));
+		cudaMemset(c->Ex64, 0, (ng + 3 * (int64_t) g.nx) * sizeof(double));
+		cudaMemset(c->Ey64, 0, (ng + 3 * (int64_t) g.nx) * sizeof(double));
+	}
+	else
+	{
+		AL(c->phi32, ng * sizeof(float));
+		AL(c->E32, ng * sizeof(float2));
+		AL(c->spec32, ng / g.nx * nh * sizeof(float2));
+		AL(c->twx32, g.nx / 2 * sizeof(float2));
+		AL(c->twy32, g.ny / 2 * sizeof(float2));
+		cudaMemset(c->E32, 0, ng * sizeof(float2));
+	}
+#undef AL
+	cudaMemset(c->rho, 0, ng * sizeof(long long));
+	cudaMemset(c->status, 0, sizeof(uint32_t));
+	{
+		// Green's function cosines as MFT_init computes them
+		// (solver.c:257-278) and FFT twiddles exp(-2 pi i k / n).
+		std::vector<double> cx(g.nx), cy(g.ny);
+		double ccx = 2.0 * M_PI / g.nx, ccy = 2.0 * M_PI / g.ny;
+		for(int i = 0; i < g.nx; i++) cx[i] = cos(ccx * i);
+		for(int i = 0; i < g.ny; i++) cy[i] = cos(ccy * i);
+		cudaMemcpy(c->cosx, cx.data(), g.nx * sizeof(double), cudaMemcpyHostToDevice);
+		cudaMemcpy(c->cosy, cy.data(), g.ny * sizeof(double), cudaMemcpyHostToDevice);
+		for(int dim = 0; dim < 2; dim++)
+		{
+			int n = dim == 0 ? g.nx : g.ny;
+			std::vector<double2> tw(n / 2);
+			std::vector<float2> tf(n / 2);
+			for(int k = 0; k < n / 2; k++)
+			{
+				double a = -2.0 * M_PI * k / n;
+				tw[k] = make_double2(cos(a), sin(a));
+				tf[k] = make_float2((float) cos(a), (float) sin(a));
+			}
+			if(c->precision == CPIC_FP64)
+				cudaMemcpy(dim == 0 ? c->twx64 : c->twy64, tw.data(), n / 2 * sizeof(double2),
+						cudaMemcpyHostToDevice);
+			else
+				cudaMemcpy(dim == 0 ? c->twx32 : c->twy32, tf.data(), n / 2 * sizeof(float2),
+						cudaMemcpyHostToDevice);
+		}
+	}
+	if(cudaDeviceSynchronize() != cudaSuccess) { r = CPIC_ECUDA; goto fail; }
+	*out = c;
+	return CPIC_OK;
+fail:
+	cpic_destroy(c);
+	return r;
+}
+
+CPIC_API void cpic_destroy(cpic_ctx_t *c)
+{
+	if(!c) return;
+	cudaStreamSynchronize(c->stream);
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		SpeciesHost &S = c->sp[s];
+		free_store(c, S, false);
+		free_store(c, S, true);
+		cudaFree(S.tiles.base); cudaFree(S.tiles.cap); cudaFree(S.tiles.cnt);
+		cudaFree(S.tiles.app); cudaFree(S.tiles.stay);
+		free_spill(S.spill[0]);
+		free_spill(S.spill[1]);
+	}
+	cudaFree(c->rho); cudaFree(c->phi64); cudaFree(c->Ex64); cudaFree(c->Ey64);
+	cudaFree(c->phi32); cudaFree(c->E32); cudaFree(c->spec64); cudaFree(c->spec32);
+	cudaFree(c->twx64); cudaFree(c->twy64); cudaFree(c->twx32); cudaFree(c->twy32);
+	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->mean); cudaFree(c->rho_sum);
+	cudaFree(c->status); cudaFree(c->scratch); cudaFree(c->counter);
+	if(c->stream) cudaStreamDestroy(c->stream);
+	delete c;
+}
+
+// Fixed-point scale: the largest power of two keeping every node sum (at
+// most sum_s n_s |q_s/e0|) below 2^62; the mixed form also keeps a single
+// contribution within 2^30 so that it converts through int32.
+static void update_qscale(cpic_ctx *c)
+{
+	double bound = 0.0, vmax = 0.0;
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		double vq = fabs(c->sp[s].q / c->p.e0);
+		bound += (double) c->sp[s].n * vq;
+		vmax = std::max(vmax, vq);
+	}
+	if(bound <= 0.0) bound = 1.0;
+	int k = (int) floor(62.0 - log2(bound)) - 1;
+	if(c->precision == CPIC_MIXED && vmax > 0.0)
+		k = std::min(k, (int) floor(30.0 - log2(vmax)) - 1);
+	c->qscale = ldexp(1.0, k);
+	c->qinv = ldexp(1.0, -k);
+}
+
+CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
+		const double *x, const double *y, const double *ux, const double *uy)
+{
+	if(!c || n < 0 || n >= INT32_MAX || !(m != 0.0) || c->nspecies >= kMaxSpecies)
+		return CPIC_EINVAL;
+	if(n > 0 && (!x || !y || !ux || !uy)) return CPIC_EINVAL;
+	if(c->prepared) return CPIC_ESTATE;
+	int s = c->nspecies;
+	SpeciesHost &S = c->sp[s];
+	memset((void *) &S, 0, sizeof(S));
+	S.q = q; S.m = m; S.n = n;
+	for(int64_t i = 0; i < n; i++)
+	{
+		// comm_plasma's global exchange never wraps X (comm_plasma.c:826-870)
+		if(!(x[i] >= 0.0 && x[i] <= c->p.Lx) || !std::isfinite(y[i])
+				|| !std::isfinite(ux[i]) || !std::isfinite(uy[i]))
+			return CPIC_EINVAL;
+		S.vmax = std::max(S.vmax, std::max(fabs(ux[i]), fabs(uy[i])));
+	}
+	int nt = c->ntiles;
+	CK(cudaMalloc(&S.tiles.base, nt * sizeof(int64_t)));
+	CK(cudaMalloc(&S.tiles.cap, nt * sizeof(int32_t)));
+	CK(cudaMalloc(&S.tiles.cnt, nt * sizeof(int32_t)));
+	CK(cudaMalloc(&S.tiles.app, nt * sizeof(int32_t)));
+	CK(cudaMalloc(&S.tiles.stay, nt * sizeof(int32_t)));
+	CK(cudaMemset(S.tiles.cnt, 0, nt * sizeof(int32_t)));
+	CK(cudaMemset(S.tiles.app, 0, nt * sizeof(int32_t)));
+	CK(cudaMemset(S.tiles.stay, 0, nt * sizeof(int32_t)));
+	int32_t scap = (int32_t) std::max<int64_t>(65536, n / 32);
+	int r;
+	if((r = alloc_spill(S.spill[0], scap))) return r;
+	if((r = alloc_spill(S.spill[1], scap))) return r;
+	c->nspecies++;
+
+	// staging upload in the FP64 spill layout, then a counting sort
+	Spill stg;
+	memset(&stg, 0, sizeof(stg));
+	if((r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1)))) return r;
+	cudaStream_t st = c->stream;
+	if(n > 0)
+	{
+		CK(cudaMemcpyAsync(stg.x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.y, y, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.ux, ux, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.uy, uy, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		k_iota<<<grid_blocks(n), 256, 0, st>>>(n, stg.id);
+		k_wrap_y<<<grid_blocks(n), 256, 0, st>>>(n, stg.y, c->p.Ly);
+	}
+	update_qscale(c);
+	r = rebuild_species(c, s, true, &stg, n);
+	free_spill(stg);
+	if(r) return r;
+	// halo: 1.5x the largest initial displacement per step, plus one
+	double vmax = 0.0;
+	for(int k = 0; k < c->nspecies; k++) vmax = std::max(vmax, c->sp[k].vmax);
+	if(c->p.halo <= 0)
+	{
+		int H = (int) ceil(1.5 * vmax * c->p.dt * std::max(c->g.idx, c->g.idy)) + 1;
+		H = std::max(1, std::min(H, c->g.tx));
+		c->g.halo = H;
+	}
+	return s;
+}
+
+CPIC_API int cpic_pre_step(cpic_ctx_t *c)
+{
+	if(!c) return CPIC_EINVAL;
+	if(c->prepared) return CPIC_ESTATE;
+	int r = plasma_stage_async(c, true);
+	if(r) return r;
+	if((r = field_stage_async(c))) return r;
+	if((r = check_status(c))) return r;
+	if((r = rebuild_if_spilled(c))) return r;
+	c->prepared = true;
+	c->iter = 0;
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_stage_field_E(cpic_ctx_t *c)
+{
+	if(!c) return CPIC_EINVAL;
+	int r = field_stage_async(c);
+	if(r) return r;
+	return check_status(c);
+}
+
+CPIC_API int cpic_stage_plasma(cpic_ctx_t *c)
+{
+	if(!c) return CPIC_EINVAL;
+	if(!c->prepared) return CPIC_ESTATE;
+	int r = plasma_stage_async(c, false);
+	if(r) return r;
+	c->iter++;
+	if((r = check_status(c))) return r;
+	return rebuild_if_spilled(c);
+}
+
+CPIC_API int cpic_step(cpic_ctx_t *c)
+{
+	if(!c) return CPIC_EINVAL;
+	if(!c->prepared) return CPIC_ESTATE;
+	if(c->p.cycles > 0 && c->iter >= c->p.cycles) return CPIC_EDONE;
+	int r = field_stage_async(c);
+	if(r) return r;
+	if((r = plasma_stage_async(c, false))) return r;
+	c->iter++;
+	if((r = check_status(c))) return r;
+	return rebuild_if_spilled(c);
+}
+
+CPIC_API int cpic_run(cpic_ctx_t *c, int64_t nsteps)
+{
+	if(!c) return CPIC_EINVAL;
+	if(!c->prepared) return CPIC_ESTATE;
+	for(int64_t k = 0; k < nsteps; k++)
+	{
+		if(c->p.cycles > 0 && c->iter >= c->p.cycles) return CPIC_EDONE;
+		int r = field_stage_async(c);
+		if(r) return r;
+		if((r = plasma_stage_async(c, false))) return r;
+		c->iter++;
+		if((k & 15) == 15 || k + 1 == nsteps)
+		{
+			if((r = check_status(c))) return r;
+			if((r = rebuild_if_spilled(c))) return r;
+		}
+	}
+	return CPIC_OK;
+}
+
+CPIC_API int64_t cpic_iter(const cpic_ctx_t *c) { return c ? c->iter : -1; }
+CPIC_API int cpic_nspecies(const cpic_ctx_t *c) { return c ? c->nspecies : 0; }
+CPIC_API int64_t cpic_species_count(const cpic_ctx_t *c, int s)
+{
+	if(!c || s < 0 || s >= c->nspecies) return -1;
+	return c->sp[s].n;
+}
+
+CPIC_API int cpic_get_particles(cpic_ctx_t *c, int s, double *x, double *y, double *ux,
+		double *uy)
+{
+	if(!c || s < 0 || s >= c->nspecies) return CPIC_EINVAL;
+	int64_t n = c->sp[s].n;
+	int r = ensure_scratch(c, 4 * (size_t) std::max<int64_t>(n, 1));
+	if(r) return r;
+	cudaStream_t st = c->stream;
+	double *d = c->scratch;
+	bool by_id = c->precision == CPIC_FP64 || c->p.track_ids;
+	CK(cudaMemsetAsync(c->counter, 0, sizeof(int32_t), st));
+	PushArgs a = make_args(c, c->spill_cur);
+	if(c->precision == CPIC_MIXED)
+		k_download<Mix><<<c->ntiles, 256, 0, st>>>(a, s, d, d + n, d + 2 * n, d + 3 * n,
+				c->counter, by_id);
+	else
+		k_download<F64><<<c->ntiles, 256, 0, st>>>(a, s, d, d + n, d + 2 * n, d + 3 * n,
+				c->counter, by_id);
+	CK(cudaGetLastError());
+	double *outs[4] = {x, y, ux, uy};
+	for(int k = 0; k < 4; k++)
+		if(outs[k] && n > 0)
+			CK(cudaMemcpyAsync(outs[k], d + k * n, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_set_particles(cpic_ctx_t *c, int s, const double *x, const double *y,
+		const double *ux, const double *uy)
+{
+	if(!c || s < 0 || s >= c->nspecies) return CPIC_EINVAL;
+	if(!x || !y || !ux || !uy) return CPIC_EINVAL;
+	SpeciesHost &S = c->sp[s];
+	int64_t n = S.n;
+	for(int64_t i = 0; i < n; i++)
+		if(!(x[i] >= 0.0 && x[i] <= c->p.Lx) || !(y[i] >= 0.0 && y[i] <= c->p.Ly))
+			return CPIC_EINVAL;
+	Spill stg;
+	memset(&stg, 0, sizeof(stg));
+	int r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1));
+	if(r) return r;
+	cudaStream_t st = c->stream;
+	if(n > 0)
+	{
+		CK(cudaMemcpyAsync(stg.x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.y, y, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.ux, ux, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.uy, uy, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		k_iota<<<grid_blocks(n), 256, 0, st>>>(n, stg.id);
+	}
+	r = rebuild_species(c, s, true, &stg, n);
+	free_spill(stg);
+	return r;
+}
+
+CPIC_API int cpic_gather_E(cpic_ctx_t *c, int s, double *ex, double *ey)
+{
+	if(!c || s < 0 || s >= c->nspecies) return CPIC_EINVAL;
+	if(c->precision == CPIC_MIXED && !c->p.track_ids) return CPIC_EINVAL;
+	int64_t n = c->sp[s].n;
+	int r = ensure_scratch(c, 2 * (size_t) std::max<int64_t>(n, 1));
+	if(r) return r;
+	cudaStream_t st = c->stream;
+	SpeciesHost &S = c->sp[s];
+	if(c->precision == CPIC_MIXED)
+		launch_gather_mix_tiles(c->g, S.mix, S.tiles.base, S.tiles.cnt, c->ntiles, c->E32,
+				c->scratch, c->scratch + n, st);
+	else
+		launch_gather_f64_tiles(c->g, S.f64, S.tiles.base, S.tiles.cnt, c->ntiles, c->Ex64,
+				c->Ey64, c->scratch, c->scratch + n, st);
+	CK(cudaGetLastError());
+	if(ex) CK(cudaMemcpyAsync(ex, c->scratch, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+	if(ey) CK(cudaMemcpyAsync(ey, c->scratch + n, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_get_rho(cpic_ctx_t *c, double *rho)
+{
+	if(!c || !rho) return CPIC_EINVAL;
+	int64_t ng = (int64_t) c->g.nx * c->g.ny;
+	int r = ensure_scratch(c, ng);
+	if(r) return r;
+	k_rho_to_f64<<<grid_blocks(ng), 256, 0, c->stream>>>(ng, c->rho, c->qinv, c->scratch);
+	CK(cudaMemcpyAsync(rho, c->scratch, ng * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_set_rho(cpic_ctx_t *c, const double *rho)
+{
+	if(!c || !rho) return CPIC_EINVAL;
+	int64_t ng = (int64_t) c->g.nx * c->g.ny;
+	int r = ensure_scratch(c, ng);
+	if(r) return r;
+	CK(cudaMemcpyAsync(c->scratch, rho, ng * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+	k_f64_to_rho<<<grid_blocks(ng), 256, 0, c->stream>>>(ng, c->scratch, c->qscale, c->rho);
+	CK(cudaStreamSynchronize(c->stream));
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_get_phi(cpic_ctx_t *c, double *phi)
+{
+	if(!c || !phi) return CPIC_EINVAL;
+	int64_t ng = (int64_t) c->g.nx * c->g.ny;
+	if(c->precision == CPIC_FP64)
+	{
+		CK(cudaMemcpy(phi, c->phi64, ng * sizeof(double), cudaMemcpyDeviceToHost));
+		return CPIC_OK;
+	}
+	std::vector<float> tmp(ng);
+	CK(cudaMemcpy(tmp.data(), c->phi32, ng * sizeof(float), cudaMemcpyDeviceToHost));
+	for(int64_t i = 0; i < ng; i++) phi[i] = tmp[i];
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_get_E(cpic_ctx_t *c, double *ex, double *ey)
+{
+	if(!c) return CPIC_EINVAL;
+	int64_t nx = c->g.nx, ng = nx * c->g.ny, ne = ng + nx;
+	CK(cudaStreamSynchronize(c->stream));
+	if(c->precision == CPIC_FP64)
+	{
+		if(ex) CK(cudaMemcpy(ex, c->Ex64, ne * sizeof(double), cudaMemcpyDeviceToHost));
+		if(ey) CK(cudaMemcpy(ey, c->Ey64, ne * sizeof(double), cudaMemcpyDeviceToHost));
+		return CPIC_OK;
+	}
+	std::vector<float2> tmp(ng);
+	CK(cudaMemcpy(tmp.data(), c->E32, ng * sizeof(float2), cudaMemcpyDeviceToHost));
+	for(int64_t i = 0; i < ne; i++)
+	{
+		float2 v = tmp[i % ng];
+		if(ex) ex[i] = v.x;
+		if(ey) ey[i] = v.y;
+	}
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_set_E(cpic_ctx_t *c, const double *ex, const double *ey)
+{
+	if(!c || !ex || !ey) return CPIC_EINVAL;
+	int64_t nx = c->g.nx, ng = nx * c->g.ny, ne = ng + nx;
+	if(c->precision == CPIC_FP64)
+	{
+		CK(cudaMemcpy(c->Ex64, ex, ne * sizeof(double), cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(c->Ey64, ey, ne * sizeof(double), cudaMemcpyHostToDevice));
+		return CPIC_OK;
+	}
+	std::vector<float2> tmp(ng);
+	for(int64_t i = 0; i < ng; i++) tmp[i] = make_float2((float) ex[i], (float) ey[i]);
+	CK(cudaMemcpy(c->E32, tmp.data(), ng * sizeof(float2), cudaMemcpyHostToDevice));
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_cell_counts(cpic_ctx_t *c, int64_t *counts)
+{
+	if(!c || !counts) return CPIC_EINVAL;
+	int64_t ng = (int64_t) c->g.nx * c->g.ny;
+	int r = ensure_scratch(c, ng);
+	if(r) return r;
+	cudaStream_t st = c->stream;
+	unsigned long long *d = (unsigned long long *) c->scratch;
+	CK(cudaMemsetAsync(d, 0, ng * sizeof(unsigned long long), st));
+	PushArgs a = make_args(c, c->spill_cur);
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		if(c->precision == CPIC_MIXED)
+			k_cell_counts<Mix><<<c->ntiles, 256, 0, st>>>(a, s, d);
+		else
+			k_cell_counts<F64><<<c->ntiles, 256, 0, st>>>(a, s, d);
+	}
+	CK(cudaGetLastError());
+	CK(cudaMemcpyAsync(counts, d, ng * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_diag(cpic_ctx_t *c, double *out)
+{
+	if(!c || !out) return CPIC_EINVAL;
+	int nt = c->ntiles, ny = c->g.ny;
+	size_t need = std::max<size_t>(2 * (size_t) ny, 3 * (size_t) nt);
+	int r = ensure_scratch(c, need);
+	if(r) return r;
+	cudaStream_t st = c->stream;
+	std::vector<double> h(need);
+	k_field_energy<<<ny, 256, 0, st>>>(c->g, c->Ex64, c->Ey64,
+			c->precision == CPIC_MIXED ? c->E32 : nullptr, c->rho, c->scratch);
+	CK(cudaMemcpyAsync(h.data(), c->scratch, 2 * ny * sizeof(double), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	double we = 0.0, q = 0.0;
+	for(int i = 0; i < ny; i++) { we += h[2 * i]; q += h[2 * i + 1]; }
+	double ke = 0.0, px = 0.0, py = 0.0;
+	PushArgs a = make_args(c, c->spill_cur);
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		if(c->precision == CPIC_MIXED)
+			k_kinetic<Mix><<<nt, 256, 0, st>>>(a, s, c->sp[s].m, c->scratch);
+		else
+			k_kinetic<F64><<<nt, 256, 0, st>>>(a, s, c->sp[s].m, c->scratch);
+		CK(cudaMemcpyAsync(h.data(), c->scratch, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		for(int t = 0; t < nt; t++) { ke += h[3 * t]; px += h[3 * t + 1]; py += h[3 * t + 2]; }
+	}
+	out[0] = 0.5 * c->p.e0 * we * c->g.dx * c->g.dy;
+	out[1] = ke;
+	out[2] = q * c->qinv * c->g.dx * c->g.dy;
+	out[3] = px;
+	out[4] = py;
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_field_energy(cpic_ctx_t *c, double *out)
+{
+	if(!c || !out) return CPIC_EINVAL;
+	int ny = c->g.ny;
+	int r = ensure_scratch(c, 2 * (size_t) ny);
+	if(r) return r;
+	cudaStream_t st = c->stream;
+	std::vector<double> h(2 * (size_t) ny);
+	k_field_energy<<<ny, 256, 0, st>>>(c->g, c->Ex64, c->Ey64,
+			c->precision == CPIC_MIXED ? c->E32 : nullptr, c->rho, c->scratch);
+	CK(cudaMemcpyAsync(h.data(), c->scratch, 2 * ny * sizeof(double), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	double we = 0.0, q = 0.0;
+	for(int i = 0; i < ny; i++) { we += h[2 * i]; q += h[2 * i + 1]; }
+	out[0] = 0.5 * c->p.e0 * we * c->g.dx * c->g.dy;
+	out[1] = q * c->qinv * c->g.dx * c->g.dy;
+	return CPIC_OK;
+}
+
+CPIC_API uint32_t cpic_status_bits(cpic_ctx_t *c)
+{
+	if(!c) return 0xffffffffu;
+	uint32_t st = 0;
+	cudaStreamSynchronize(c->stream);
+	cudaMemcpy(&st, c->status, sizeof(st), cudaMemcpyDeviceToHost);
+	return st;
+}
+
+CPIC_API int cpic_time_steps(cpic_ctx_t *c, int64_t nsteps, double *ms_total, double *ms_plasma,
+		double *ms_field)
+{
+	if(!c || nsteps <= 0) return CPIC_EINVAL;
+	if(!c->prepared) return CPIC_ESTATE;
+	cudaStream_t st = c->stream;
+	std::vector<cudaEvent_t> ev(2 * nsteps + 2 + 2 * nsteps);
+	for(auto &e : ev) CK(cudaEventCreate(&e));
+	int r = CPIC_OK;
+	CK(cudaStreamSynchronize(st));
+	CK(cudaEventRecord(ev[0], st));
+	for(int64_t k = 0; k < nsteps; k++)
+	{
+		cudaEvent_t f0 = ev[2 + 2 * nsteps + 2 * k];
+		cudaEvent_t f1 = ev[2 + 2 * nsteps + 2 * k + 1];
+		CK(cudaEventRecord(f0, st));
+		if((r = field_stage_async(c))) break;
+		CK(cudaEventRecord(f1, st));
+		if((r = plasma_stage_async(c, false, ev[2 + 2 * k], ev[2 + 2 * k + 1]))) break;
+		c->iter++;
+	}
+	CK(cudaEventRecord(ev[1], st));
+	CK(cudaEventSynchronize(ev[1]));
+	float tot = 0.0f;
+	double sp = 0.0, sf = 0.0;
+	CK(cudaEventElapsedTime(&tot, ev[0], ev[1]));
+	for(int64_t k = 0; k < nsteps; k++)
+	{
+		float a = 0.0f, b = 0.0f;
+		CK(cudaEventElapsedTime(&a, ev[2 + 2 * k], ev[2 + 2 * k + 1]));
+		CK(cudaEventElapsedTime(&b, ev[2 + 2 * nsteps + 2 * k], ev[2 + 2 * nsteps + 2 * k + 1]));
+		sp += a;
+		sf += b;
+	}
+	for(auto &e : ev) cudaEventDestroy(e);
+	if(ms_total) *ms_total = tot;
+	if(ms_plasma) *ms_plasma = sp;
+	if(ms_field) *ms_field = sf;
+	if(r) return r;
+	if((r = check_status(c))) return r;
+	return rebuild_if_spilled(c);
+}
+
+CPIC_API int cpic_tile_info(const cpic_ctx_t *c, int32_t *out)
+{
+	if(!c || !out) return CPIC_EINVAL;
+	out[0] = c->g.tx;
+	out[1] = c->g.ty;
+	out[2] = c->g.halo;
+	out[3] = 25;
+	return CPIC_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,216 @@
+// cpic_fft.cuh -- periodic FFT Poisson solver for power-of-two grids,
+// templated on the real type (double for the FP64 form, float for the
+// mixed form).
+//
+// Replaces MFT_solve (src/solver.c:465-509): phi = IFFT(G * FFT(rho)) / (nx
+// ny) with G(kx,ky) = 1 / (2 (cos(2 pi kx/nx) + cos(2 pi ky/ny)) - 4) and
+// G(0,0) = 0 (solver.c:269-280).  Three kernels, all working in shared
+// memory with Stockham radix-2 passes (self-sorting, no bit reversal):
+//   rows_fwd : two real rows packed as one complex row, FFT along x, split
+//              into the two half spectra (nx/2+1 bins each);
+//   cols     : a block of spectrum columns, FFT along y, multiply by G,
+//              inverse FFT along y (the Green's function never leaves
+//              shared memory);
+//   rows_inv : two half spectra packed into one Hermitian-extended row,
+//              inverse FFT, real and imaginary parts are the two phi rows,
+//              divided by nx*ny as MFT_normalize does (solver.c:366).
+#pragma once
+#include <cuda_runtime.h>
+#include "cpic_common.cuh"
+
+namespace cpic {
+
+template <typename T> struct Cx;
+template <> struct Cx<double> { typedef double2 t; };
+template <> struct Cx<float> { typedef float2 t; };
+
+template <typename C>
+__device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C>
+__device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C>
+__device__ __forceinline__ C cmul(C a, C b)
+{
+	C r;
+	r.x = a.x * b.x - a.y * b.y;
+	r.y = a.x * b.y + a.y * b.x;
+	return r;
+}
+
+// nb independent length-n sequences stored back to back in `a`; `b` is
+// scratch of the same size.  tw[k] = exp(-2 pi i k / n), k < n/2.  sign
+// -1 forward, +1 inverse (unnormalised).  Returns the buffer holding the
+// result.  Must be called by the whole block.
+template <typename C>
+__device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *tw)
+{
+	int half = n >> 1;
+	int total = half * nb;
+	for(int s = 0; s < log2n; s++)
+	{
+		int Ns = 1 << s;
+		int tshift = log2n - 1 - s;     // n / (2 Ns) = 2^tshift
+		for(int idx = threadIdx.x; idx < total; idx += blockDim.x)
+		{
+			int seq = idx >> (log2n - 1);
+			int j = idx & (half - 1);
+			C *x = a + seq * n;
+			C *y = b + seq * n;
+			int k = j & (Ns - 1);
+			C a0 = x[j];
+			C a1 = x[j + half];
+			C w = tw[k << tshift];
+			if(sign > 0) w.y = -w.y;
+			a1 = cmul(a1, w);
+			int o = ((j - k) << 1) + k;
+			y[o] = cadd(a0, a1);
+			y[o + Ns] = csub(a0, a1);
+		}
+		__syncthreads();
+		C *t = a; a = b; b = t;
+	}
+	return a;
+}
+
+// rho (fixed point, ny x nx) -> spec (ny x (nx/2+1)).  One block per row
+// pair.  value = (double) acc * qinv - mean (mean may be null).
+template <typename T>
+__global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, double qinv,
+		const double *mean, typename Cx<T>::t *spec, const typename Cx<T>::t *tw)
+{
+	typedef typename Cx<T>::t C;
+	extern __shared__ unsigned char smem_raw[];
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + nx;
+	int r0 = 2 * blockIdx.x;
+	int nh = nx / 2 + 1;
+	double m = mean ? *mean : 0.0;
+	for(int i = threadIdx.x; i < nx; i += blockDim.x)
+	{
+		double va = (double) rho[(int64_t) r0 * nx + i] * qinv - m;
+		double vb = (double) rho[(int64_t) (r0 + 1) * nx + i] * qinv - m;
+		C z; z.x = (T) va; z.y = (T) vb;
+		a[i] = z;
+	}
+	__syncthreads();
+	C *Z = fft_smem<C>(a, b, nx, log2nx, 1, -1, tw);
+	for(int k = threadIdx.x; k < nh; k += blockDim.x)
+	{
+		C p = Z[k];
+		C q = Z[(nx - k) & (nx - 1)];
+		q.y = -q.y;                          // conj(Z[-k])
+		C A, B;
+		A.x = (p.x + q.x) * (T) 0.5;
+		A.y = (p.y + q.y) * (T) 0.5;
+		// (p - q) / (2i) = -i (p - q) / 2
+		B.x = (p.y - q.y) * (T) 0.5;
+		B.y = -(p.x - q.x) * (T) 0.5;
+		spec[(int64_t) r0 * nh + k] = A;
+		spec[(int64_t) (r0 + 1) * nh + k] = B;
+	}
+}
+
+// Columns [c0, c0 + cb) of spec: FFT along y, multiply by G, inverse FFT.
+template <typename T>
+__global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *spec,
+		const typename Cx<T>::t *tw, const double *cosx, const double *cosy)
+{
+	typedef typename Cx<T>::t C;
+	extern __shared__ unsigned char smem_raw[];
+	int nh = nx / 2 + 1;
+	int c0 = blockIdx.x * cb;
+	int ncol = min(cb, nh - c0);
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + (size_t) cb * ny;
+	for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
+	{
+		int row = idx / ncol, c = idx - row * ncol;
+		a[c * ny + row] = spec[(int64_t) row * nh + c0 + c];
+	}
+	__syncthreads();
+	C *X = fft_smem<C>(a, b, ny, log2ny, ncol, -1, tw);
+	for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
+	{
+		int c = idx / ny, row = idx - c * ny;
+		int kx = c0 + c;
+		double G = (kx == 0 && row == 0) ? 0.0 : 1.0 / (2.0 * (cosx[kx] + cosy[row]) - 4.0);
+		C v = X[idx];
+		v.x = v.x * (T) G;
+		v.y = v.y * (T) G;
+		X[idx] = v;
+	}
+	__syncthreads();
+	C *Y = (X == a) ? b : a;
+	C *R = fft_smem<C>(X, Y, ny, log2ny, ncol, +1, tw);
+	for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
+	{
+		int row = idx / ncol, c = idx - row * ncol;
+		spec[(int64_t) row * nh + c0 + c] = R[c * ny + row];
+	}
+}
+
+// spec -> phi (ny x nx real).  One block per row pair.
+template <typename T>
+__global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<T>::t *spec,
+		const typename Cx<T>::t *tw, T *phi)
+{
+	typedef typename Cx<T>::t C;
+	extern __shared__ unsigned char smem_raw[];
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + nx;
+	int r0 = 2 * blockIdx.x;
+	int nh = nx / 2 + 1;
+	for(int k = threadIdx.x; k < nh; k += blockDim.x)
+	{
+		C A = spec[(int64_t) r0 * nh + k];
+		C B = spec[(int64_t) (r0 + 1) * nh + k];
+		if(k == 0 || k == nx / 2)
+		{
+			// c2r uses only the real part of the DC and Nyquist bins
+			C y; y.x = A.x; y.y = B.x;
+			a[k] = y;
+		}
+		else
+		{
+			C y;
+			y.x = A.x - B.y; y.y = A.y + B.x;     // A + iB
+			a[k] = y;
+			y.x = A.x + B.y; y.y = B.x - A.y;     // conj(A) + i conj(B)
+			a[nx - k] = y;
+		}
+	}
+	__syncthreads();
+	C *Y = fft_smem<C>(a, b, nx, log2nx, 1, +1, tw);
+	T N = (T) ((double) nx * (double) ny);
+	for(int i = threadIdx.x; i < nx; i += blockDim.x)
+	{
+		C v = Y[i];
+		phi[(int64_t) r0 * nx + i] = v.x / N;
+		phi[(int64_t) (r0 + 1) * nx + i] = v.y / N;
+	}
+}
+
+template <typename T>
+static void poisson_launch(const Grid &g, const long long *rho, double qinv, const double *mean,
+		typename Cx<T>::t *spec, const typename Cx<T>::t *twx, const typename Cx<T>::t *twy,
+		const double *cosx, const double *cosy, T *phi, cudaStream_t s)
+{
+	typedef typename Cx<T>::t C;
+	int log2nx = 0, log2ny = 0;
+	while((1 << log2nx) < g.nx) log2nx++;
+	while((1 << log2ny) < g.ny) log2ny++;
+	int rthreads = g.nx / 2 < 512 ? (g.nx / 2 < 32 ? 32 : g.nx / 2) : 512;
+	size_t rsm = 2 * (size_t) g.nx * sizeof(C);
+	k_rows_fwd<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, rho, qinv, mean, spec, twx);
+	int nh = g.nx / 2 + 1;
+	// columns per block: fill up to 128 KB of shared memory (two buffers)
+	int cb = (int) ((128 * 1024) / (2 * (size_t) g.ny * sizeof(C)));
+	if(cb < 1) cb = 1;
+	if(cb > nh) cb = nh;
+	size_t csm = 2 * (size_t) cb * g.ny * sizeof(C);
+	int cthreads = 512;
+	k_cols<T><<<(nh + cb - 1) / cb, cthreads, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy);
+	k_rows_inv<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, phi);
+}
+
+} // namespace cpic

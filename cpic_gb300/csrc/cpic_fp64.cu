@@ -1,0 +1,102 @@
+// cpic_fp64.cu -- FP64 ("plain") form of the step.  Compiled with
+// --fmad=false so that every FP64 expression rounds exactly as the
+// reference's C code does (no FMA contraction).
+#include "cpic_common.cuh"
+#include "cpic_push.cuh"
+#include "cpic_fft.cuh"
+
+namespace cpic {
+
+// field_E_compute, src/field.c:358-416: E = -grad(phi) by central
+// differences, rows 0..ny (row ny is the south ghost), periodic through the
+// phi ghosts (src/comm_field.c:140-201), which equals periodic indexing.
+__global__ void k_E_f64(Grid g, const double *phi, double *Ex, double *Ey)
+{
+	int64_t total = (int64_t) (g.ny + 1) * g.nx;
+	double dx2 = 2 * g.dx, dy2 = 2 * g.dy;
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
+			i += (int64_t) gridDim.x * blockDim.x)
+	{
+		int iy = (int) (i / g.nx), ix = (int) (i - (int64_t) iy * g.nx);
+		int y0 = iy - 1 < 0 ? g.ny - 1 : iy - 1;
+		int y1 = (iy + 1) % g.ny;
+		int yc = iy % g.ny;
+		int x0 = (ix + g.nx - 1) % g.nx;
+		int x1 = (ix + 1) % g.nx;
+		Ey[i] = (phi[(int64_t) y0 * g.nx + ix] - phi[(int64_t) y1 * g.nx + ix]) / dy2;
+		Ex[i] = (phi[(int64_t) yc * g.nx + x0] - phi[(int64_t) yc * g.nx + x1]) / dx2;
+	}
+}
+
+void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s)
+{
+	int64_t total = (int64_t) (g.ny + 1) * g.nx;
+	int blocks = (int) ((total + 255) / 256);
+	if(blocks > 4096) blocks = 4096;
+	k_E_f64<<<blocks, 256, 0, s>>>(g, phi, Ex, Ey);
+}
+
+// E at every particle (interpolate_f2p_E), written by particle id.  One
+// block per tile.
+__global__ void k_gather_f64(Grid g, StoreF64 st, const int64_t *base, const int32_t *cnt,
+		const double *Ex, const double *Ey, double *ex_out, double *ey_out)
+{
+	int t = blockIdx.x;
+	int n = cnt[t];
+	int64_t b = base[t];
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		double w[4];
+		int i0x, i0y;
+		double x = st.x[b + i], y = st.y[b + i];
+		F64::weights(g, x, y, w, i0x, i0y);
+		i0x = min(max(i0x, 0), g.nx);
+		i0y = min(max(i0y, 0), g.ny);
+		double ex, ey;
+		F64::gather(Ex, Ey, g, w, i0x, i0y, ex, ey);
+		int id = st.id[b + i];
+		ex_out[id] = ex;
+		ey_out[id] = ey;
+	}
+}
+
+void launch_gather_f64_tiles(const Grid &g, const StoreF64 &st, const int64_t *base,
+		const int32_t *cnt, int ntiles, const double *Ex, const double *Ey,
+		double *ex_out, double *ey_out, cudaStream_t s)
+{
+	k_gather_f64<<<ntiles, 256, 0, s>>>(g, st, base, cnt, Ex, Ey, ex_out, ey_out);
+}
+
+void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+{
+	static bool init = false;
+	if(!init)
+	{
+		cudaFuncSetAttribute(k_push<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		init = true;
+	}
+	dim3 grid(ntiles, a.nspecies);
+	k_push<F64><<<grid, kPushThreads, smem, s>>>(a);
+}
+
+void launch_spill_f64(const SpillArgs &a, cudaStream_t s)
+{
+	k_spill<F64><<<152, kPushThreads, 0, s>>>(a);
+}
+
+void launch_poisson_f64(const Grid &g, const long long *rho, double qinv, double *,
+		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
+		const double *cosy, double *phi, cudaStream_t s)
+{
+	static bool init = false;
+	if(!init)
+	{
+		cudaFuncSetAttribute(k_rows_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		cudaFuncSetAttribute(k_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		cudaFuncSetAttribute(k_rows_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		init = true;
+	}
+	poisson_launch<double>(g, rho, qinv, nullptr, spec, twx, twy, cosx, cosy, phi, s);
+}
+
+} // namespace cpic

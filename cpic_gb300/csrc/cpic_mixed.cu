@@ -1,0 +1,103 @@
+// cpic_mixed.cu -- mixed-precision form: int32 cell + FP32 offset, FP32
+// velocity, E and FFT; charge reduction in 64-bit fixed point, k=0 removal
+// in FP64.  FMA contraction is allowed here.
+#include "cpic_common.cuh"
+#include "cpic_push.cuh"
+#include "cpic_fft.cuh"
+
+namespace cpic {
+
+// E = -grad(phi), FP32, periodic (field_E_compute, src/field.c:358-416),
+// stored as (Ex, Ey) pairs for the per-tile shared-memory stage.
+__global__ void k_E_mix(Grid g, const float *phi, float2 *E)
+{
+	int64_t total = (int64_t) g.ny * g.nx;
+	float rdx2 = (float) (1.0 / (2 * g.dx)), rdy2 = (float) (1.0 / (2 * g.dy));
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
+			i += (int64_t) gridDim.x * blockDim.x)
+	{
+		int iy = (int) (i / g.nx), ix = (int) (i - (int64_t) iy * g.nx);
+		int y0 = iy == 0 ? g.ny - 1 : iy - 1;
+		int y1 = iy + 1 == g.ny ? 0 : iy + 1;
+		int x0 = ix == 0 ? g.nx - 1 : ix - 1;
+		int x1 = ix + 1 == g.nx ? 0 : ix + 1;
+		float2 e;
+		e.x = (phi[(int64_t) iy * g.nx + x0] - phi[(int64_t) iy * g.nx + x1]) * rdx2;
+		e.y = (phi[(int64_t) y0 * g.nx + ix] - phi[(int64_t) y1 * g.nx + ix]) * rdy2;
+		E[i] = e;
+	}
+}
+
+void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s)
+{
+	int64_t total = (int64_t) g.ny * g.nx;
+	int blocks = (int) ((total + 255) / 256);
+	if(blocks > 4096) blocks = 4096;
+	k_E_mix<<<blocks, 256, 0, s>>>(g, phi, E);
+}
+
+// E at every particle of a mixed store, by particle id (ids required).
+__global__ void k_gather_mix(Grid g, StoreMix st, const int64_t *base, const int32_t *cnt,
+		const float2 *E, double *ex_out, double *ey_out)
+{
+	int t = blockIdx.x;
+	int n = cnt[t];
+	int64_t b = base[t];
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		int c = st.cell[b + i];
+		int cx = c % g.nx, cy = c / g.nx;
+		int x1 = cx + 1 == g.nx ? 0 : cx + 1;
+		int y1 = cy + 1 == g.ny ? 0 : cy + 1;
+		float ox = st.ox[b + i], oy = st.oy[b + i];
+		float dxo = 1.0f - ox, dyo = 1.0f - oy;
+		float2 e00 = E[(int64_t) cy * g.nx + cx], e01 = E[(int64_t) y1 * g.nx + cx];
+		float2 e10 = E[(int64_t) cy * g.nx + x1], e11 = E[(int64_t) y1 * g.nx + x1];
+		float ex = dxo * dyo * e00.x + dxo * oy * e01.x + ox * dyo * e10.x + ox * oy * e11.x;
+		float ey = dxo * dyo * e00.y + dxo * oy * e01.y + ox * dyo * e10.y + ox * oy * e11.y;
+		int id = st.id ? st.id[b + i] : (int) (b + i);
+		ex_out[id] = ex;
+		ey_out[id] = ey;
+	}
+}
+
+void launch_gather_mix_tiles(const Grid &g, const StoreMix &st, const int64_t *base,
+		const int32_t *cnt, int ntiles, const float2 *E, double *ex_out, double *ey_out,
+		cudaStream_t s)
+{
+	k_gather_mix<<<ntiles, 256, 0, s>>>(g, st, base, cnt, E, ex_out, ey_out);
+}
+
+void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+{
+	static bool init = false;
+	if(!init)
+	{
+		cudaFuncSetAttribute(k_push<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		init = true;
+	}
+	dim3 grid(ntiles, a.nspecies);
+	k_push<Mix><<<grid, kPushThreads, smem, s>>>(a);
+}
+
+void launch_spill_mix(const SpillArgs &a, cudaStream_t s)
+{
+	k_spill<Mix><<<152, kPushThreads, 0, s>>>(a);
+}
+
+void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const double *mean,
+		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
+		const double *cosy, float *phi, cudaStream_t s)
+{
+	static bool init = false;
+	if(!init)
+	{
+		cudaFuncSetAttribute(k_rows_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		cudaFuncSetAttribute(k_cols<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		cudaFuncSetAttribute(k_rows_inv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		init = true;
+	}
+	poisson_launch<float>(g, rho, qinv, mean, spec, twx, twy, cosx, cosy, phi, s);
+}
+
+} // namespace cpic

@@ -1,0 +1,538 @@
+// cpic_push.cuh -- the fused particle kernel: field gather, Boris push,
+// move, periodic wrap, re-bin and charge deposit, for one tile per block.
+//
+// Replaces, per step: interpolate_f2p_E (src/interpolate.c:349-404),
+// plist_update_r / boris_rotation / move (src/mover.c:22-188), the local
+// comm_plasma re-bin and periodic_boundary (src/comm_plasma.c:695-885,
+// 1087-1142), interpolate_p2f_rho (src/interpolate.c:282-346) and the rho
+// ghost fold (src/comm_field.c:52-136).
+//
+// Two forms share the kernel skeleton:
+//   F64 : positions and velocities in FP64, exact reference arithmetic
+//         (this header is compiled with --fmad=false for it); E read from
+//         global memory with the reference's index arithmetic, quirks
+//         included.
+//   Mix : int32 cell + FP32 offset, FP32 velocity; E staged per tile in
+//         shared memory.
+#pragma once
+#include "cpic_common.cuh"
+
+namespace cpic {
+
+struct Out {
+	int dest;           // destination tile
+	int rx, ry;         // new cell relative to the tile origin (unwrapped)
+	long long w[4];     // fixed-point deposit w00, w01, w10, w11
+	int quirk;          // F64: position exactly on the upper boundary
+	int qx, qy;         // F64 quirk: raw node indices
+	uint32_t err;       // ST_* bits: velocity above umax, non-finite state
+};
+
+// =================================================================== F64
+
+struct F64 {
+	struct Rec { double x, y, ux, uy; int32_t id; };
+
+	static __device__ __forceinline__ Rec load(const PushArgs &a, int s, int64_t i)
+	{
+		const StoreF64 &st = a.f64[s];
+		Rec r;
+		r.x = st.x[i]; r.y = st.y[i]; r.ux = st.ux[i]; r.uy = st.uy[i];
+		r.id = st.id[i];
+		return r;
+	}
+
+	static __device__ __forceinline__ void store(const PushArgs &a, int s, int64_t i, const Rec &r)
+	{
+		const StoreF64 &st = a.f64[s];
+		st.x[i] = r.x; st.y[i] = r.y; st.ux[i] = r.ux; st.uy[i] = r.uy;
+		st.id[i] = r.id;
+	}
+
+	// relative_position_grid, interpolate.c:38-66 (field origin 0 on one
+	// rank).  The cell index is floor() converted to int, as
+	// vf64_to_vi64 does for in-range values (simd_avx2.h:238-248).
+	static __device__ __forceinline__ double rel_pos(double x, double dx, double idx, int &i0)
+	{
+		double block_delta = x - 0.0;
+		double block_rel = block_delta * idx;
+		double block_start = floor(block_rel);
+		i0 = (int) block_start;
+		double grid_delta = block_delta - block_start * dx;
+		return grid_delta * idx;
+	}
+
+	// weights(), interpolate.c:77-100 (Y uses dx[X], interpolate.c:88)
+	// and linear_interpolation, interpolate.c:11-32.
+	static __device__ __forceinline__ void weights(const Grid &g, double x, double y,
+			double w[4], int &i0x, int &i0y)
+	{
+		double rx = rel_pos(x, g.dx, g.idx, i0x);
+		double ry = rel_pos(y, g.dx, g.idy, i0y);
+		double delx = 1.0 - rx, dely = 1.0 - ry;
+		w[0] = delx * dely;
+		w[1] = delx * ry;
+		w[2] = rx * dely;
+		w[3] = rx * ry;
+	}
+
+	// interpolate_f2p, interpolate.c:102-155: nodes (i0x,i0y) (i0x,i1y)
+	// (i1x,i0y) (i1x,i1y) in that order; i1x wraps, i1y is the ghost row.
+	// Index = iy * nx + ix exactly as MAT_XY on E (real_shape[X] = nx).
+	static __device__ __forceinline__ void gather(const double *Ex, const double *Ey,
+			const Grid &g, const double w[4], int i0x, int i0y, double &ex, double &ey)
+	{
+		int64_t nx = g.nx;
+		int i1x = i0x + 1, i1y = i0y + 1;
+		if(i1x >= g.nx) i1x -= g.nx;
+		int64_t n00 = (int64_t) i0y * nx + i0x, n01 = (int64_t) i1y * nx + i0x;
+		int64_t n10 = (int64_t) i0y * nx + i1x, n11 = (int64_t) i1y * nx + i1x;
+		double v;
+		v  = w[0] * Ex[n00];
+		v += w[1] * Ex[n01];
+		v += w[2] * Ex[n10];
+		v += w[3] * Ex[n11];
+		ex = v;
+		v  = w[0] * Ey[n00];
+		v += w[1] * Ey[n01];
+		v += w[2] * Ey[n10];
+		v += w[3] * Ey[n11];
+		ey = v;
+	}
+
+	// Everything for one particle.  tx0/ty0: origin of the tile the
+	// particle is processed in (deposit frame).
+	static __device__ __forceinline__ Out push(const PushArgs &a, int s, Rec &r,
+			int tx0, int ty0, const void *)
+	{
+		const Grid &g = a.g;
+		const SpeciesStep &sp = a.sp[s];
+		Out o;
+		o.err = 0;
+		o.quirk = 0;
+		double w[4];
+		int i0x, i0y;
+		weights(g, r.x, r.y, w, i0x, i0y);
+		if(i0x < 0 || i0y < 0 || i0x > g.nx || i0y > g.ny)
+		{
+			o.err |= ST_RANGE;
+			i0x = min(max(i0x, 0), g.nx - 1);
+			i0y = min(max(i0y, 0), g.ny - 1);
+		}
+		double ex, ey;
+		gather(a.Ex64, a.Ey64, g, w, i0x, i0y, ex, ey);
+
+		// boris_rotation, mover.c:22-70, with B = (0, 0, Bz): the terms
+		// multiplied by the exact zeros t[X], t[Y], s[X], s[Y] vanish
+		// exactly, leaving these operations in the same order.
+		double dtqm2 = sp.dtqm2;
+		double vmx = r.ux + dtqm2 * ex;
+		double vmy = r.uy + dtqm2 * ey;
+		double vpx = vmy * sp.tz + vmx;
+		double vpy = vmy - vmx * sp.tz;
+		double vlx = vpy * sp.sz + vmx;
+		double vly = vmy - vpx * sp.sz;
+		double ux = vlx + dtqm2 * ex;
+		double uy = vly + dtqm2 * ey;
+
+		// check_velocity, mover.c:97-137
+		if(fabs(ux) > sp.umax_x || fabs(uy) > sp.umax_y)
+			o.err |= ST_UMAX;
+		if(!isfinite(ux) || !isfinite(uy))
+			o.err |= ST_NAN;
+
+		double x = r.x, y = r.y;
+		if(a.iter != 0)
+		{
+			// move, mover.c:74-82
+			x += ux * a.dt;
+			y += uy * a.dt;
+		}
+		// periodic_boundary_ppack, comm_plasma.c:725-747 (X then Y)
+		if(x >= g.Lx) x -= g.Lx;
+		else if(x < 0.0) x += g.Lx;
+		if(y >= g.Ly) y -= g.Ly;
+		else if(y < 0.0) y += g.Ly;
+		if(!isfinite(x) || !isfinite(y))
+		{
+			o.err |= ST_NAN;
+			x = 0.0; y = 0.0;
+		}
+		r.x = x; r.y = y; r.ux = ux; r.uy = uy;
+
+		// deposit weights of the new position (interpolate_p2f,
+		// interpolate.c:161-276), value w * (-q/e0) in fixed point
+		weights(g, x, y, w, i0x, i0y);
+		for(int c = 0; c < 4; c++)
+			o.w[c] = __double2ll_rn(w[c] * sp.qfix);
+		if(i0x >= g.nx || i0y >= g.ny || i0x < 0 || i0y < 0)
+		{
+			// x == L or y == L after the wrap: keep the reference's
+			// node indices (column nx is FFT padding, row ny+1 is
+			// outside rho).
+			o.quirk = 1;
+			o.qx = i0x; o.qy = i0y;
+			int cx = min(max(i0x, 0), g.nx - 1), cy = min(max(i0y, 0), g.ny - 1);
+			o.dest = tile_of(g, cx, cy);
+			o.rx = 0; o.ry = 0;
+			return o;
+		}
+		o.dest = tile_of(g, i0x, i0y);
+		int rx = i0x - tx0, ry = i0y - ty0;
+		if(rx > g.nx / 2) rx -= g.nx;
+		else if(rx < -g.nx / 2) rx += g.nx;
+		if(ry > g.ny / 2) ry -= g.ny;
+		else if(ry < -g.ny / 2) ry += g.ny;
+		o.rx = rx; o.ry = ry;
+		return o;
+	}
+
+	// Deposit for the quirk positions, with the reference's node indices:
+	// contributions to column nx (FFT padding) and row ny+1 are dropped,
+	// row ny folds into row 0.
+	static __device__ __forceinline__ void dep_quirk(const PushArgs &a, const Out &o)
+	{
+		const Grid &g = a.g;
+		int i0x = o.qx, i0y = o.qy;
+		int i1x = i0x + 1; if(i1x >= g.nx) i1x -= g.nx;
+		int i1y = i0y + 1;
+		int xs[4] = {i0x, i0x, i1x, i1x};
+		int ys[4] = {i0y, i1y, i0y, i1y};
+		for(int c = 0; c < 4; c++)
+		{
+			int x = xs[c], y = ys[c];
+			if(x < 0 || x >= g.nx || y < 0 || y > g.ny) continue;
+			if(y == g.ny) y = 0;
+			atomicAdd((unsigned long long *) &a.rho[(int64_t) y * g.nx + x],
+					(unsigned long long) o.w[c]);
+		}
+	}
+
+	// Spill records are stored in this same layout.
+	static __device__ __forceinline__ Rec from_spill(const Spill &S, int64_t k, const Grid &)
+	{
+		Rec r;
+		r.x = S.x[k]; r.y = S.y[k]; r.ux = S.ux[k]; r.uy = S.uy[k]; r.id = S.id[k];
+		return r;
+	}
+
+	static __device__ __forceinline__ void to_spill_vals(const Rec &r, const Grid &,
+			double &x, double &y, double &ux, double &uy)
+	{
+		x = r.x; y = r.y; ux = r.ux; uy = r.uy;
+	}
+
+	static __device__ __forceinline__ int cell_of(const Rec &r, const Grid &g, int &cx, int &cy)
+	{
+		double w[4];
+		weights(g, r.x, r.y, w, cx, cy);
+		return 0;
+	}
+};
+
+// =================================================================== Mix
+
+struct Mix {
+	struct Rec { int32_t cell; float ox, oy, ux, uy; int32_t id; };
+
+	static __device__ __forceinline__ Rec load(const PushArgs &a, int s, int64_t i)
+	{
+		const StoreMix &st = a.mix[s];
+		Rec r;
+		r.cell = st.cell[i];
+		r.ox = st.ox[i]; r.oy = st.oy[i];
+		r.ux = st.ux[i]; r.uy = st.uy[i];
+		r.id = st.id ? st.id[i] : 0;
+		return r;
+	}
+
+	static __device__ __forceinline__ void store(const PushArgs &a, int s, int64_t i, const Rec &r)
+	{
+		const StoreMix &st = a.mix[s];
+		st.cell[i] = r.cell;
+		st.ox[i] = r.ox; st.oy[i] = r.oy;
+		st.ux[i] = r.ux; st.uy[i] = r.uy;
+		if(st.id) st.id[i] = r.id;
+	}
+
+	// Et: (TX+1) x (TY+1) shared tile of E at the tile's nodes, or null
+	// for the global field (spill records).
+	static __device__ __forceinline__ Out push(const PushArgs &a, int s, Rec &r,
+			int tx0, int ty0, const void *Etile)
+	{
+		const Grid &g = a.g;
+		const SpeciesStep &sp = a.sp[s];
+		Out o;
+		o.err = 0;
+		o.quirk = 0;
+		int cx = r.cell % g.nx, cy = r.cell / g.nx;
+		float ox = r.ox, oy = r.oy;
+		float dxo = 1.0f - ox, dyo = 1.0f - oy;
+		float w00 = dxo * dyo, w01 = dxo * oy, w10 = ox * dyo, w11 = ox * oy;
+		float2 e00, e01, e10, e11;
+		if(Etile)
+		{
+			const float2 *Et = (const float2 *) Etile;
+			int W = g.tx + 1;
+			int lx = cx - tx0, ly = cy - ty0;
+			if(lx < 0 || ly < 0 || lx >= g.tx || ly >= g.ty)
+			{
+				o.err |= ST_RANGE;
+				lx = min(max(lx, 0), g.tx - 1);
+				ly = min(max(ly, 0), g.ty - 1);
+			}
+			const float2 *p = Et + ly * W + lx;
+			e00 = p[0]; e01 = p[W]; e10 = p[1]; e11 = p[W + 1];
+		}
+		else
+		{
+			int x1 = cx + 1 == g.nx ? 0 : cx + 1;
+			int y1 = cy + 1 == g.ny ? 0 : cy + 1;
+			e00 = a.E32[(int64_t) cy * g.nx + cx];
+			e01 = a.E32[(int64_t) y1 * g.nx + cx];
+			e10 = a.E32[(int64_t) cy * g.nx + x1];
+			e11 = a.E32[(int64_t) y1 * g.nx + x1];
+		}
+		float ex = w00 * e00.x + w01 * e01.x + w10 * e10.x + w11 * e11.x;
+		float ey = w00 * e00.y + w01 * e01.y + w10 * e10.y + w11 * e11.y;
+
+		// Boris with B along z (same structure as the FP64 form)
+		float dtqm2 = sp.dtqm2_f;
+		float vmx = r.ux + dtqm2 * ex;
+		float vmy = r.uy + dtqm2 * ey;
+		float vpx = vmx + vmy * sp.tz_f;
+		float vpy = vmy - vmx * sp.tz_f;
+		float ux = vmx + vpy * sp.sz_f + dtqm2 * ex;
+		float uy = vmy - vpx * sp.sz_f + dtqm2 * ey;
+		if(fabsf(ux) > (float) sp.umax_x || fabsf(uy) > (float) sp.umax_y)
+			o.err |= ST_UMAX;
+		if(!isfinite(ux) || !isfinite(uy))
+		{
+			o.err |= ST_NAN;
+			ux = 0.0f; uy = 0.0f;
+		}
+		int sx = 0, sy = 0;
+		if(a.iter != 0)
+		{
+			ox += ux * a.cdx_f;
+			oy += uy * a.cdy_f;
+			float fx = floorf(ox), fy = floorf(oy);
+			ox -= fx; oy -= fy;
+			sx = (int) fx; sy = (int) fy;
+			if(ox >= 1.0f) { ox -= 1.0f; sx += 1; }
+			if(oy >= 1.0f) { oy -= 1.0f; sy += 1; }
+		}
+		int ncx = wrapi(cx + sx, g.nx), ncy = wrapi(cy + sy, g.ny);
+		r.cell = ncy * g.nx + ncx;
+		r.ox = ox; r.oy = oy; r.ux = ux; r.uy = uy;
+
+		dxo = 1.0f - ox; dyo = 1.0f - oy;
+		float q = sp.qfix_f;
+		o.w[0] = (long long) __float2int_rn(dxo * dyo * q);
+		o.w[1] = (long long) __float2int_rn(dxo * oy * q);
+		o.w[2] = (long long) __float2int_rn(ox * dyo * q);
+		o.w[3] = (long long) __float2int_rn(ox * oy * q);
+		o.dest = tile_of(g, ncx, ncy);
+		if(Etile)
+		{
+			o.rx = cx - tx0 + sx;
+			o.ry = cy - ty0 + sy;
+		}
+		else
+		{
+			o.rx = ncx - tx0;
+			o.ry = ncy - ty0;
+		}
+		return o;
+	}
+
+	static __device__ __forceinline__ void dep_quirk(const PushArgs &, const Out &) {}
+
+	static __device__ __forceinline__ int cell_of(const Rec &r, const Grid &g, int &cx, int &cy)
+	{
+		cx = r.cell % g.nx;
+		cy = r.cell / g.nx;
+		return 0;
+	}
+
+	static __device__ __forceinline__ Rec from_spill(const Spill &S, int64_t k, const Grid &g)
+	{
+		Rec r;
+		double px = S.x[k] * g.idx, py = S.y[k] * g.idy;
+		double fx = floor(px), fy = floor(py);
+		int cx = wrapi((int) fx, g.nx), cy = wrapi((int) fy, g.ny);
+		float ox = (float) (px - fx), oy = (float) (py - fy);
+		if(ox >= 1.0f) { ox = 0.0f; cx = wrapi(cx + 1, g.nx); }
+		if(oy >= 1.0f) { oy = 0.0f; cy = wrapi(cy + 1, g.ny); }
+		r.cell = cy * g.nx + cx;
+		r.ox = ox; r.oy = oy;
+		r.ux = (float) S.ux[k]; r.uy = (float) S.uy[k];
+		r.id = S.id[k];
+		return r;
+	}
+
+	static __device__ __forceinline__ void to_spill_vals(const Rec &r, const Grid &g,
+			double &x, double &y, double &ux, double &uy)
+	{
+		int cx = r.cell % g.nx, cy = r.cell / g.nx;
+		x = ((double) cx + (double) r.ox) * g.dx;
+		y = ((double) cy + (double) r.oy) * g.dy;
+		ux = r.ux; uy = r.uy;
+	}
+};
+
+// ============================================================== kernels
+
+// One block per (tile, species).  Dynamic shared memory: the W x W
+// fixed-point accumulator (W = T + 2H + 1) followed, for the mixed form,
+// by the (TX+1) x (TY+1) E tile.
+template <class F>
+__global__ void __launch_bounds__(kPushThreads)
+k_push(const PushArgs a)
+{
+	extern __shared__ __align__(16) unsigned char smem[];
+	__shared__ int warp_tot[kPushThreads / 32];
+	const Grid &g = a.g;
+	const int s = blockIdx.y;
+	const int t = blockIdx.x;
+	const Tiles &T = a.tiles[s];
+	const int H = g.halo;
+	const int W = g.tx + 2 * H + 1;
+	long long *acc = reinterpret_cast<long long *>(smem);
+	float2 *Et = reinterpret_cast<float2 *>(acc + W * W);
+	const int tx0 = (t % g.ntx) * g.tx, ty0 = (t / g.ntx) * g.ty;
+
+	for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+		acc[i] = 0;
+	const void *Etile = nullptr;
+	if(a.E32)
+	{
+		int WE = g.tx + 1;
+		for(int i = threadIdx.x; i < WE * (g.ty + 1); i += blockDim.x)
+		{
+			int lx = i % WE, ly = i / WE;
+			int gx = tx0 + lx, gy = ty0 + ly;
+			if(gx >= g.nx) gx -= g.nx;
+			if(gy >= g.ny) gy -= g.ny;
+			Et[i] = a.E32[(int64_t) gy * g.nx + gx];
+		}
+		Etile = Et;
+	}
+	__syncthreads();
+
+	const int n = T.cnt[t];
+	const int64_t base = T.base[t];
+	int wptr = 0;
+	const unsigned lane_lt = (1u << (threadIdx.x & 31)) - 1;
+
+	for(int c0 = 0; c0 < n; c0 += kChunk)
+	{
+		typename F::Rec rec[kPPT];
+		#pragma unroll
+		for(int k = 0; k < kPPT; k++)
+		{
+			int i = c0 + k * kPushThreads + threadIdx.x;
+			if(i < n) rec[k] = F::load(a, s, base + i);
+		}
+		// all loads of the chunk precede the in-place writes below
+		__syncthreads();
+		#pragma unroll
+		for(int k = 0; k < kPPT; k++)
+		{
+			int i = c0 + k * kPushThreads + threadIdx.x;
+			bool valid = i < n;
+			Out o;
+			o.dest = t;
+			o.err = 0;
+			o.quirk = 0;
+			if(valid)
+			{
+				o = F::push(a, s, rec[k], tx0, ty0, Etile);
+				if(o.err) set_status(a.status, o.err);
+				if(o.quirk)
+					F::dep_quirk(a, o);
+				else
+					dep_tile(acc, W, H, g, tx0, ty0, o.rx, o.ry,
+							o.w[0], o.w[1], o.w[2], o.w[3], a.rho);
+			}
+			bool stay = valid && o.dest == t;
+			int tot;
+			int off = block_scan_flag(stay, warp_tot, &tot);
+			if(stay)
+				F::store(a, s, base + wptr + off, rec[k]);
+			bool move = valid && o.dest != t;
+			unsigned movers = __ballot_sync(0xffffffffu, move);
+			if(move)
+			{
+				int64_t slot = reserve_slot(a.tiles[s], o.dest, movers);
+				if(slot >= 0)
+					F::store(a, s, slot, rec[k]);
+				else
+				{
+					double x, y, ux, uy;
+					F::to_spill_vals(rec[k], g, x, y, ux, uy);
+					spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id, a.status);
+				}
+			}
+			(void) lane_lt;
+			wptr += tot;
+		}
+		__syncthreads();
+	}
+	if(threadIdx.x == 0)
+		T.stay[t] = wptr;
+	__syncthreads();
+	flush_tile(acc, W, H, g, tx0, ty0, a.rho);
+}
+
+// Generic pass over the spill list: records with no tile of their own
+// (the particle store overflowed).  E is read from global memory and the
+// deposit goes straight to global rho.  Records are placed in their tile
+// when it has room, else appended to spill_out.
+template <class F>
+__global__ void __launch_bounds__(kPushThreads)
+k_spill(const SpillArgs sa)
+{
+	const PushArgs &a = sa.p;
+	const Grid &g = a.g;
+	for(int s = 0; s < a.nspecies; s++)
+	{
+		const Spill &S = sa.spill_in[s];
+		int ns = *S.count;
+		if(ns > S.capacity) ns = S.capacity;
+		for(int64_t k0 = (int64_t) blockIdx.x * blockDim.x; k0 < ns;
+				k0 += (int64_t) gridDim.x * blockDim.x)
+		{
+			int64_t k = k0 + threadIdx.x;
+			bool valid = k < ns;
+			typename F::Rec r;
+			Out o;
+			o.dest = 0;
+			if(valid)
+			{
+				r = F::from_spill(S, k, g);
+				o = F::push(a, s, r, 0, 0, nullptr);
+				if(o.err) set_status(a.status, o.err);
+				if(o.quirk)
+					F::dep_quirk(a, o);
+				else
+					dep_global(a.rho, g, o.rx, o.ry, o.w[0], o.w[1], o.w[2], o.w[3]);
+			}
+			unsigned act = __ballot_sync(0xffffffffu, valid);
+			if(valid)
+			{
+				int64_t slot = reserve_slot(a.tiles[s], o.dest, act);
+				if(slot >= 0)
+					F::store(a, s, slot, r);
+				else
+				{
+					double x, y, ux, uy;
+					F::to_spill_vals(r, g, x, y, ux, uy);
+					spill_push(a.spill_out[s], x, y, ux, uy, r.id, a.status);
+				}
+			}
+		}
+	}
+}
+
+} // namespace cpic
