@@ -10,11 +10,14 @@
 // that find no room go to a spill list that a generic kernel keeps pushing
 // until the host rebuilds the layout with a full counting sort.
 //
-// Charge deposit: 64-bit two's-complement fixed point.  Every contribution
-// w*(-q/e0) is rounded to an integer multiple of 1/qscale and summed with
-// integer adds, in shared memory per tile and in global memory across
-// tiles.  Integer sums are exact and order independent, so the deposit is
-// deterministic without float atomics.
+// Charge deposit: 64-bit two's-complement fixed point in global memory.
+// Every contribution is an integer; integer sums are exact and order
+// independent, so the deposit is deterministic without float atomics.
+// FP64 form: each contribution w*(-q/e0) is rounded to a multiple of
+// 1/qscale and summed per tile in 64-bit shared memory.  Mixed form: the
+// weights w are rounded to multiples of 2^-kWeightBits and summed per tile
+// in 32-bit shared memory (folded into a 64-bit shadow before any sum can
+// wrap); the species charge multiplies the tile sums at the flush.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -25,6 +28,8 @@ constexpr int kMaxSpecies = 8;
 constexpr int kPushThreads = 256;
 constexpr int kPPT = 4;                       // particles per thread per chunk
 constexpr int kChunk = kPushThreads * kPPT;   // particles per chunk
+constexpr int kWeightBits = 20;
+constexpr int kFoldChunks = 2;   // kFoldChunks * kChunk * 2^kWeightBits <= 2^31
 
 // Device status bits (sticky until the host clears them).
 enum : uint32_t {
@@ -69,6 +74,8 @@ struct Grid {
 	int tx, ty;          // tile size in cells
 	int ntx, nty;        // tiles per dimension
 	int halo;            // deposit halo in cells
+	int lnx, lny;        // log2 of nx, ny (grids are powers of two)
+	int ltx, lty;        // log2 of tx, ty
 	double dx, dy, idx, idy, Lx, Ly;
 };
 
@@ -78,8 +85,9 @@ struct SpeciesStep {
 	double tz, sz;       // Boris t and s for B along z (mover.c:45-51)
 	double umax_x, umax_y;
 	double qfix;         // fixed-point units per unit of w: -q/e0 * qscale
-	float qfix_f;        // same, FP32 (mixed form)
+	double wq_scale;     // mixed: fixed-point units per integer weight unit
 	float dtqm2_f, tz_f, sz_f;
+	float umax_x_f, umax_y_f;
 };
 
 struct PushArgs {
@@ -106,10 +114,10 @@ struct SpillArgs {
 
 // ---------------------------------------------------------------- helpers
 
-__device__ __forceinline__ int wrapi(int i, int n)
+// Periodic wrap for a power-of-two extent (any sign of i).
+__device__ __forceinline__ int wrap2(int i, int n)
 {
-	i %= n;
-	return i < 0 ? i + n : i;
+	return i & (n - 1);
 }
 
 __device__ __forceinline__ void set_status(uint32_t *st, uint32_t bit)
@@ -120,83 +128,65 @@ __device__ __forceinline__ void set_status(uint32_t *st, uint32_t bit)
 // Tile index of a cell.
 __device__ __forceinline__ int tile_of(const Grid &g, int cx, int cy)
 {
-	return (cy / g.ty) * g.ntx + (cx / g.tx);
+	return ((cy >> g.lty) << (g.lnx - g.ltx)) + (cx >> g.ltx);
 }
 
-// Shared-memory fixed-point deposit of one particle's four node weights,
-// with the node frame relative to the tile origin (tile-local cell rx, ry,
-// may lie in the halo).  Falls back to global atomics outside the halo.
-template <int NONE>
-struct Deposit {};
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+	return (1u << (threadIdx.x & 31)) - 1u;
+}
 
+__device__ __forceinline__ void red_global(long long *p, long long v)
+{
+	atomicAdd((unsigned long long *) p, (unsigned long long) v);
+}
+
+// Fixed-point deposit of one particle's four node values straight into the
+// global accumulator (cell (cx, cy) may be outside the grid: wrapped).
 __device__ __forceinline__ void
 dep_global(long long *rho, const Grid &g, int cx, int cy,
 		long long w00, long long w01, long long w10, long long w11)
 {
-	int x0 = wrapi(cx, g.nx), y0 = wrapi(cy, g.ny);
-	int x1 = x0 + 1 == g.nx ? 0 : x0 + 1;
-	int y1 = y0 + 1 == g.ny ? 0 : y0 + 1;
-	atomicAdd((unsigned long long *) &rho[(int64_t) y0 * g.nx + x0], (unsigned long long) w00);
-	atomicAdd((unsigned long long *) &rho[(int64_t) y1 * g.nx + x0], (unsigned long long) w01);
-	atomicAdd((unsigned long long *) &rho[(int64_t) y0 * g.nx + x1], (unsigned long long) w10);
-	atomicAdd((unsigned long long *) &rho[(int64_t) y1 * g.nx + x1], (unsigned long long) w11);
+	int x0 = wrap2(cx, g.nx), y0 = wrap2(cy, g.ny);
+	int x1 = wrap2(x0 + 1, g.nx), y1 = wrap2(y0 + 1, g.ny);
+	red_global(&rho[((int64_t) y0 << g.lnx) + x0], w00);
+	red_global(&rho[((int64_t) y1 << g.lnx) + x0], w01);
+	red_global(&rho[((int64_t) y0 << g.lnx) + x1], w10);
+	red_global(&rho[((int64_t) y1 << g.lnx) + x1], w11);
 }
 
-// acc is a W x W shared array covering nodes [t0 - H, t0 + T + H] of the
-// tile; (rx, ry) is the cell relative to the tile origin.
-__device__ __forceinline__ void
-dep_tile(long long *acc, int W, int H, const Grid &g, int tx0, int ty0,
-		int rx, int ry, long long w00, long long w01, long long w10, long long w11,
-		long long *rho)
-{
-	int lx = rx + H, ly = ry + H;
-	if(lx >= 0 && ly >= 0 && lx + 1 < W && ly + 1 < W)
-	{
-		long long *a = acc + ly * W + lx;
-		atomicAdd((unsigned long long *) &a[0], (unsigned long long) w00);
-		atomicAdd((unsigned long long *) &a[W], (unsigned long long) w01);
-		atomicAdd((unsigned long long *) &a[1], (unsigned long long) w10);
-		atomicAdd((unsigned long long *) &a[W + 1], (unsigned long long) w11);
-	}
-	else
-	{
-		dep_global(rho, g, tx0 + rx, ty0 + ry, w00, w01, w10, w11);
-	}
-}
-
-// Add a tile's shared accumulator into the global fixed-point rho.
-__device__ __forceinline__ void
-flush_tile(const long long *acc, int W, int H, const Grid &g, int tx0, int ty0,
-		long long *rho)
-{
-	for(int i = threadIdx.x; i < W * W; i += blockDim.x)
-	{
-		long long v = acc[i];
-		if(v == 0) continue;
-		int gx = wrapi(tx0 - H + i % W, g.nx);
-		int gy = wrapi(ty0 - H + i / W, g.ny);
-		atomicAdd((unsigned long long *) &rho[(int64_t) gy * g.nx + gx], (unsigned long long) v);
-	}
-}
-
-// Reserve a slot in the destination tile for a mover: lanes with the same
-// destination share one atomic.  Returns the slot or -1 when the tile is
-// full (the caller spills).
+// Global node index of shared accumulator entry i (frame origin t0 - H).
 __device__ __forceinline__ int64_t
-reserve_slot(const Tiles &T, int dest, unsigned active)
+frame_node(const Grid &g, int W, int H, int tx0, int ty0, int i)
 {
-	unsigned peers = __match_any_sync(active, dest);
-	int leader = __ffs(peers) - 1;
+	int gx = wrap2(tx0 - H + i % W, g.nx);
+	int gy = wrap2(ty0 - H + i / W, g.ny);
+	return ((int64_t) gy << g.lnx) + gx;
+}
+
+// Warp-aggregated slot reservation for movers: one atomic per distinct
+// destination tile in the warp.  Must be called by the whole warp; returns
+// the slot within the destination tile for lanes with `move`, else -1.
+__device__ __forceinline__ int
+warp_reserve(int32_t *app, bool move, int dest)
+{
+	unsigned pending = __ballot_sync(0xffffffffu, move);
+	int slot = -1;
 	int lane = threadIdx.x & 31;
-	int rank = __popc(peers & ((1u << lane) - 1));
-	int first = 0;
-	if(lane == leader)
-		first = atomicAdd(&T.app[dest], __popc(peers));
-	first = __shfl_sync(peers, first, leader);
-	int slot = first + rank;
-	if(slot >= T.cap[dest])
-		return -1;
-	return T.base[dest] + slot;
+	while(pending)
+	{
+		int leader = __ffs(pending) - 1;
+		int d = __shfl_sync(0xffffffffu, dest, leader);
+		unsigned grp = __ballot_sync(0xffffffffu, move && dest == d);
+		int first = 0;
+		if(lane == leader)
+			first = atomicAdd(&app[d], __popc(grp));
+		first = __shfl_sync(0xffffffffu, first, leader);
+		if(grp & (1u << lane))
+			slot = first + __popc(grp & lanemask_lt());
+		pending &= ~grp;
+	}
+	return slot;
 }
 
 // Append a record to a spill list; false when the list is full.
@@ -215,50 +205,21 @@ spill_push(const Spill &S, double x, double y, double ux, double uy, int32_t id,
 	return true;
 }
 
-// Block-wide exclusive scan of one flag per thread (kPushThreads threads).
-// Returns this thread's offset; *total receives the block sum.  Uses
-// `warp_tot` (kPushThreads/32 ints of shared memory); contains two
-// __syncthreads.
-__device__ __forceinline__ int
-block_scan_flag(bool flag, int *warp_tot, int *total)
-{
-	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	unsigned b = __ballot_sync(0xffffffffu, flag);
-	int in_warp = __popc(b & ((1u << lane) - 1));
-	if(lane == 0) warp_tot[warp] = __popc(b);
-	__syncthreads();
-	int off = 0, tot = 0;
-	#pragma unroll
-	for(int w = 0; w < kPushThreads / 32; w++)
-	{
-		int c = warp_tot[w];
-		off += w < warp ? c : 0;
-		tot += c;
-	}
-	__syncthreads();
-	*total = tot;
-	return off + in_warp;
-}
-
 } // namespace cpic
 
 // Launchers implemented in the per-precision translation units.
 namespace cpic {
 void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
 void launch_spill_f64(const SpillArgs &a, cudaStream_t s);
-void launch_gather_f64(const Grid &g, const StoreF64 &st, int64_t n, const double *Ex,
-		const double *Ey, double *ex_out, double *ey_out, cudaStream_t s);
 void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s);
-void launch_poisson_f64(const Grid &g, const long long *rho, double qinv, double *rho_out,
+void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
 		const double *cosy, double *phi, cudaStream_t s);
 
 void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
-void launch_gather_mix(const Grid &g, const StoreMix &st, int64_t n, const float2 *E,
-		double *ex_out, double *ey_out, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
-void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const double *mean,
+void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
 		const double *cosy, float *phi, cudaStream_t s);
 } // namespace cpic

@@ -263,13 +263,14 @@ __global__ void k_field_energy(Grid g, const double *Ex, const double *Ey, const
 	}
 }
 
-// Exact int64 sum of rho, then the mean as FP64 (mixed form k=0 removal).
-__global__ void k_rho_mean(int64_t n, const long long *rho, long long *sum, double qinv,
-		double *mean)
+// Exact int64 sum of rho (the k = 0 mode of the mixed form, removed in FP64
+// before the FP32 transform).  Integer adds: any order gives the same sum.
+__global__ void k_rho_sum(int64_t n, const long long *rho, long long *sum)
 {
-	__shared__ long long sh[1024];
+	__shared__ long long sh[256];
 	long long v = 0;
-	for(int64_t i = threadIdx.x; i < n; i += blockDim.x)
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+			i += (int64_t) gridDim.x * blockDim.x)
 		v += rho[i];
 	sh[threadIdx.x] = v;
 	__syncthreads();
@@ -279,10 +280,7 @@ __global__ void k_rho_mean(int64_t n, const long long *rho, long long *sum, doub
 		__syncthreads();
 	}
 	if(threadIdx.x == 0)
-	{
-		*sum = sh[0];
-		*mean = (double) sh[0] * qinv / (double) n;
-	}
+		atomicAdd((unsigned long long *) sum, (unsigned long long) sh[0]);
 }
 
 __global__ void k_rho_to_f64(int64_t n, const long long *rho, double qinv, double *out)
@@ -385,20 +383,21 @@ static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
 		st.umax_y = c->g.ny * c->g.dy / p.dt;
 		double vq = -q / p.e0;
 		st.qfix = vq * c->qscale;
-		st.qfix_f = (float) st.qfix;
+		st.wq_scale = st.qfix * ldexp(1.0, -kWeightBits);
 		st.dtqm2_f = (float) st.dtqm2;
 		st.tz_f = (float) st.tz;
 		st.sz_f = (float) st.sz;
+		st.umax_x_f = (float) st.umax_x;
+		st.umax_y_f = (float) st.umax_y;
 	}
 }
 
 static size_t push_smem(const cpic_ctx *c)
 {
 	int W = c->g.tx + 2 * c->g.halo + 1;
-	size_t sm = (size_t) W * W * sizeof(long long);
 	if(c->precision == CPIC_MIXED)
-		sm += (size_t) (c->g.tx + 1) * (c->g.ty + 1) * sizeof(float2);
-	return sm;
+		return Mix::smem_bytes(W, c->g.tx);
+	return F64::smem_bytes(W, c->g.tx);
 }
 
 static int check_status(cpic_ctx *c)
@@ -645,6 +644,7 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 			sa.p.sp[s].dtqm2 = 0.0; sa.p.sp[s].tz = 0.0; sa.p.sp[s].sz = 0.0;
 			sa.p.sp[s].dtqm2_f = 0.0f; sa.p.sp[s].tz_f = 0.0f; sa.p.sp[s].sz_f = 0.0f;
 			sa.p.sp[s].umax_x = INFINITY; sa.p.sp[s].umax_y = INFINITY;
+			sa.p.sp[s].umax_x_f = INFINITY; sa.p.sp[s].umax_y_f = INFINITY;
 		}
 		sa.p.iter = 0;
 	}
@@ -678,14 +678,15 @@ static int field_stage_async(cpic_ctx *c)
 	if(c->precision == CPIC_MIXED)
 	{
 		int64_t ng = (int64_t) c->g.nx * c->g.ny;
-		k_rho_mean<<<1, 1024, 0, st>>>(ng, c->rho, c->rho_sum, c->qinv, c->mean);
-		launch_poisson_mix(c->g, c->rho, c->qinv, c->mean, c->spec32, c->twx32, c->twy32,
+		CK(cudaMemsetAsync(c->rho_sum, 0, sizeof(long long), st));
+		k_rho_sum<<<grid_blocks(ng, 256, 2 * 152), 256, 0, st>>>(ng, c->rho, c->rho_sum);
+		launch_poisson_mix(c->g, c->rho, c->qinv, c->rho_sum, c->spec32, c->twx32, c->twy32,
 				c->cosx, c->cosy, c->phi32, st);
 		launch_E_mix(c->g, c->phi32, c->E32, st);
 	}
 	else
 	{
-		launch_poisson_f64(c->g, c->rho, c->qinv, nullptr, c->spec64, c->twx64, c->twy64,
+		launch_poisson_f64(c->g, c->rho, c->qinv, c->spec64, c->twx64, c->twy64,
 				c->cosx, c->cosy, c->phi64, st);
 		launch_E_f64(c->g, c->phi64, c->Ex64, c->Ey64, st);
 	}
@@ -763,6 +764,8 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	g.tx = T; g.ty = TY;
 	g.ntx = g.nx / T; g.nty = g.ny / TY;
 	g.halo = p->halo > 0 ? p->halo : 2;
+	g.lnx = ilog2(g.nx); g.lny = ilog2(g.ny);
+	g.ltx = ilog2(T); g.lty = ilog2(TY);
 	c->ntiles = g.ntx * g.nty;
 	if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
 	{
@@ -863,21 +866,15 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 }
 
 // Fixed-point scale: the largest power of two keeping every node sum (at
-// most sum_s n_s |q_s/e0|) below 2^62; the mixed form also keeps a single
-// contribution within 2^30 so that it converts through int32.
+// most sum_s n_s |q_s/e0|, every particle's weights summing to one) below
+// 2^62, so that no partial or total sum can wrap.
 static void update_qscale(cpic_ctx *c)
 {
-	double bound = 0.0, vmax = 0.0;
+	double bound = 0.0;
 	for(int s = 0; s < c->nspecies; s++)
-	{
-		double vq = fabs(c->sp[s].q / c->p.e0);
-		bound += (double) c->sp[s].n * vq;
-		vmax = std::max(vmax, vq);
-	}
+		bound += (double) c->sp[s].n * fabs(c->sp[s].q / c->p.e0);
 	if(bound <= 0.0) bound = 1.0;
 	int k = (int) floor(62.0 - log2(bound)) - 1;
-	if(c->precision == CPIC_MIXED && vmax > 0.0)
-		k = std::min(k, (int) floor(30.0 - log2(vmax)) - 1);
 	c->qscale = ldexp(1.0, k);
 	c->qinv = ldexp(1.0, -k);
 }

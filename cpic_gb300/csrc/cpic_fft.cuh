@@ -73,10 +73,13 @@ __device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *
 }
 
 // rho (fixed point, ny x nx) -> spec (ny x (nx/2+1)).  One block per row
-// pair.  value = (double) acc * qinv - mean (mean may be null).
+// pair.  value = (double) acc * qinv - mean, where the mean (the k = 0
+// mode, removed in FP64 before the FP32 transform of the mixed form) comes
+// from the exact integer sum rsum; rsum null: no removal (FP64 form, as the
+// reference, whose G(0,0) = 0 discards the mode).
 template <typename T>
 __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, double qinv,
-		const double *mean, typename Cx<T>::t *spec, const typename Cx<T>::t *tw)
+		const long long *rsum, typename Cx<T>::t *spec, const typename Cx<T>::t *tw)
 {
 	typedef typename Cx<T>::t C;
 	extern __shared__ unsigned char smem_raw[];
@@ -84,7 +87,7 @@ __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, dou
 	C *b = a + nx;
 	int r0 = 2 * blockIdx.x;
 	int nh = nx / 2 + 1;
-	double m = mean ? *mean : 0.0;
+	double m = rsum ? (double) *rsum * qinv / ((double) nx * (double) ny) : 0.0;
 	for(int i = threadIdx.x; i < nx; i += blockDim.x)
 	{
 		double va = (double) rho[(int64_t) r0 * nx + i] * qinv - m;
@@ -191,7 +194,7 @@ __global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<T>::t *
 }
 
 template <typename T>
-static void poisson_launch(const Grid &g, const long long *rho, double qinv, const double *mean,
+static void poisson_launch(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		typename Cx<T>::t *spec, const typename Cx<T>::t *twx, const typename Cx<T>::t *twy,
 		const double *cosx, const double *cosy, T *phi, cudaStream_t s)
 {

@@ -84,7 +84,7 @@ void launch_spill_f64(const SpillArgs &a, cudaStream_t s)
 	k_spill<F64><<<152, kPushThreads, 0, s>>>(a);
 }
 
-void launch_poisson_f64(const Grid &g, const long long *rho, double qinv, double *,
+void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
 		const double *cosy, double *phi, cudaStream_t s)
 {

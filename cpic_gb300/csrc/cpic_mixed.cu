@@ -46,7 +46,7 @@ __global__ void k_gather_mix(Grid g, StoreMix st, const int64_t *base, const int
 	for(int i = threadIdx.x; i < n; i += blockDim.x)
 	{
 		int c = st.cell[b + i];
-		int cx = c % g.nx, cy = c / g.nx;
+		int cx = c & (g.nx - 1), cy = c >> g.lnx;
 		int x1 = cx + 1 == g.nx ? 0 : cx + 1;
 		int y1 = cy + 1 == g.ny ? 0 : cy + 1;
 		float ox = st.ox[b + i], oy = st.oy[b + i];
@@ -85,7 +85,7 @@ void launch_spill_mix(const SpillArgs &a, cudaStream_t s)
 	k_spill<Mix><<<152, kPushThreads, 0, s>>>(a);
 }
 
-void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const double *mean,
+void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
 		const double *cosy, float *phi, cudaStream_t s)
 {

@@ -11,27 +11,43 @@
 //   F64 : positions and velocities in FP64, exact reference arithmetic
 //         (this header is compiled with --fmad=false for it); E read from
 //         global memory with the reference's index arithmetic, quirks
-//         included.
+//         included; 64-bit fixed-point shared accumulator.
 //   Mix : int32 cell + FP32 offset, FP32 velocity; E staged per tile in
-//         shared memory.
+//         shared memory; 32-bit integer weight accumulator.
+//
+// Skeleton per block (tile t of species s): the tile's particles are read
+// in chunks of kChunk; after one barrier per chunk (every load of the chunk
+// has landed) each particle is pushed, deposited into the tile's shared
+// accumulator, and written back: stayers compacted in place through a
+// shared cursor (a warp reserves its run with one shared atomic), movers
+// appended to their destination tile (one global atomic per distinct
+// destination per warp).  In-place writes of chunk k only touch slots below
+// the end of chunk k, all of which were read before the barrier.
 #pragma once
 #include "cpic_common.cuh"
 
 namespace cpic {
 
-struct Out {
-	int dest;           // destination tile
-	int rx, ry;         // new cell relative to the tile origin (unwrapped)
-	long long w[4];     // fixed-point deposit w00, w01, w10, w11
-	int quirk;          // F64: position exactly on the upper boundary
-	int qx, qy;         // F64 quirk: raw node indices
-	uint32_t err;       // ST_* bits: velocity above umax, non-finite state
-};
-
 // =================================================================== F64
 
 struct F64 {
 	struct Rec { double x, y, ux, uy; int32_t id; };
+	static constexpr int kMinBlocks = 2;
+
+	struct Out {
+		int dest;        // destination tile
+		int rx, ry;      // new cell relative to the tile origin (unwrapped)
+		long long w[4];  // fixed-point deposit w00, w01, w10, w11
+		int quirk;       // position exactly on the upper boundary
+		int qx, qy;      // quirk: raw node indices
+		uint32_t err;
+	};
+
+	// shared memory: W x W 64-bit accumulator
+	static __host__ __device__ size_t smem_bytes(int W, int T)
+	{
+		return (size_t) W * W * sizeof(long long);
+	}
 
 	static __device__ __forceinline__ Rec load(const PushArgs &a, int s, int64_t i)
 	{
@@ -100,8 +116,8 @@ struct F64 {
 		ey = v;
 	}
 
-	// Everything for one particle.  tx0/ty0: origin of the tile the
-	// particle is processed in (deposit frame).
+	// One particle.  tx0/ty0: origin of the tile it is processed in.
+	// deposit_only: keep the state, only compute the deposit (pre-step).
 	static __device__ __forceinline__ Out push(const PushArgs &a, int s, Rec &r,
 			int tx0, int ty0, const void *)
 	{
@@ -187,28 +203,70 @@ struct F64 {
 		return o;
 	}
 
-	// Deposit for the quirk positions, with the reference's node indices:
-	// contributions to column nx (FFT padding) and row ny+1 are dropped,
-	// row ny folds into row 0.
-	static __device__ __forceinline__ void dep_quirk(const PushArgs &a, const Out &o)
+	static __device__ __forceinline__ void clear(unsigned char *sm, int W, int T)
+	{
+		long long *acc = reinterpret_cast<long long *>(sm);
+		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+			acc[i] = 0;
+	}
+
+	static __device__ __forceinline__ void fold(unsigned char *, int, int) {}
+
+	// Deposit into the tile accumulator, or globally outside the halo, or
+	// with the reference's node indices for the boundary quirk
+	// (contributions to column nx, the FFT padding, and row ny+1 are
+	// dropped; row ny folds into row 0).
+	static __device__ __forceinline__ void deposit(const PushArgs &a, int s, unsigned char *sm,
+			int W, int H, int tx0, int ty0, const Out &o)
 	{
 		const Grid &g = a.g;
-		int i0x = o.qx, i0y = o.qy;
-		int i1x = i0x + 1; if(i1x >= g.nx) i1x -= g.nx;
-		int i1y = i0y + 1;
-		int xs[4] = {i0x, i0x, i1x, i1x};
-		int ys[4] = {i0y, i1y, i0y, i1y};
-		for(int c = 0; c < 4; c++)
+		if(o.quirk)
 		{
-			int x = xs[c], y = ys[c];
-			if(x < 0 || x >= g.nx || y < 0 || y > g.ny) continue;
-			if(y == g.ny) y = 0;
-			atomicAdd((unsigned long long *) &a.rho[(int64_t) y * g.nx + x],
-					(unsigned long long) o.w[c]);
+			int i0x = o.qx, i0y = o.qy;
+			int i1x = i0x + 1; if(i1x >= g.nx) i1x -= g.nx;
+			int i1y = i0y + 1;
+			int xs[4] = {i0x, i0x, i1x, i1x};
+			int ys[4] = {i0y, i1y, i0y, i1y};
+			for(int c = 0; c < 4; c++)
+			{
+				int x = xs[c], y = ys[c];
+				if(x < 0 || x >= g.nx || y < 0 || y > g.ny) continue;
+				if(y == g.ny) y = 0;
+				red_global(&a.rho[((int64_t) y << g.lnx) + x], o.w[c]);
+			}
+			return;
+		}
+		int lx = o.rx + H, ly = o.ry + H;
+		if(sm && lx >= 0 && ly >= 0 && lx + 1 < W && ly + 1 < W)
+		{
+			long long *p = reinterpret_cast<long long *>(sm) + ly * W + lx;
+			atomicAdd((unsigned long long *) &p[0], (unsigned long long) o.w[0]);
+			atomicAdd((unsigned long long *) &p[W], (unsigned long long) o.w[1]);
+			atomicAdd((unsigned long long *) &p[1], (unsigned long long) o.w[2]);
+			atomicAdd((unsigned long long *) &p[W + 1], (unsigned long long) o.w[3]);
+		}
+		else
+			dep_global(a.rho, g, tx0 + o.rx, ty0 + o.ry, o.w[0], o.w[1], o.w[2], o.w[3]);
+	}
+
+	static __device__ __forceinline__ void flush(const PushArgs &a, int s, unsigned char *sm,
+			int W, int H, int tx0, int ty0)
+	{
+		const long long *acc = reinterpret_cast<const long long *>(sm);
+		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+		{
+			long long v = acc[i];
+			if(v != 0)
+				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)], v);
 		}
 	}
 
-	// Spill records are stored in this same layout.
+	static __device__ __forceinline__ const void *load_field(const PushArgs &, unsigned char *,
+			int, int, int, int)
+	{
+		return nullptr;
+	}
+
 	static __device__ __forceinline__ Rec from_spill(const Spill &S, int64_t k, const Grid &)
 	{
 		Rec r;
@@ -234,6 +292,22 @@ struct F64 {
 
 struct Mix {
 	struct Rec { int32_t cell; float ox, oy, ux, uy; int32_t id; };
+	static constexpr int kMinBlocks = 4;
+
+	struct Out {
+		int dest;
+		int rx, ry;
+		uint32_t wq[4];  // weights round(w * 2^kWeightBits)
+		uint32_t err;
+	};
+
+	// shared memory: W x W u32 accumulator, W x W u64 shadow, then the
+	// (T+1) x (T+1) E tile
+	static __host__ __device__ size_t smem_bytes(int W, int T)
+	{
+		return (size_t) W * W * (sizeof(uint32_t) + sizeof(unsigned long long))
+			+ (size_t) (T + 1) * (T + 1) * sizeof(float2);
+	}
 
 	static __device__ __forceinline__ Rec load(const PushArgs &a, int s, int64_t i)
 	{
@@ -255,7 +329,15 @@ struct Mix {
 		if(st.id) st.id[i] = r.id;
 	}
 
-	// Et: (TX+1) x (TY+1) shared tile of E at the tile's nodes, or null
+	// round(w * 2^kWeightBits) for w in [0, 1]: adding 2^23 puts the
+	// rounded integer in the low mantissa bits.
+	static __device__ __forceinline__ uint32_t wfix(float w)
+	{
+		float f = w * (float) (1 << kWeightBits) + 8388608.0f;
+		return __float_as_uint(f) - 0x4B000000u;
+	}
+
+	// Etile: (T+1) x (T+1) shared tile of E at the tile's nodes, or null
 	// for the global field (spill records).
 	static __device__ __forceinline__ Out push(const PushArgs &a, int s, Rec &r,
 			int tx0, int ty0, const void *Etile)
@@ -264,8 +346,7 @@ struct Mix {
 		const SpeciesStep &sp = a.sp[s];
 		Out o;
 		o.err = 0;
-		o.quirk = 0;
-		int cx = r.cell % g.nx, cy = r.cell / g.nx;
+		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
 		float ox = r.ox, oy = r.oy;
 		float dxo = 1.0f - ox, dyo = 1.0f - oy;
 		float w00 = dxo * dyo, w01 = dxo * oy, w10 = ox * dyo, w11 = ox * oy;
@@ -275,7 +356,7 @@ struct Mix {
 			const float2 *Et = (const float2 *) Etile;
 			int W = g.tx + 1;
 			int lx = cx - tx0, ly = cy - ty0;
-			if(lx < 0 || ly < 0 || lx >= g.tx || ly >= g.ty)
+			if((unsigned) lx >= (unsigned) g.tx || (unsigned) ly >= (unsigned) g.ty)
 			{
 				o.err |= ST_RANGE;
 				lx = min(max(lx, 0), g.tx - 1);
@@ -286,12 +367,11 @@ struct Mix {
 		}
 		else
 		{
-			int x1 = cx + 1 == g.nx ? 0 : cx + 1;
-			int y1 = cy + 1 == g.ny ? 0 : cy + 1;
-			e00 = a.E32[(int64_t) cy * g.nx + cx];
-			e01 = a.E32[(int64_t) y1 * g.nx + cx];
-			e10 = a.E32[(int64_t) cy * g.nx + x1];
-			e11 = a.E32[(int64_t) y1 * g.nx + x1];
+			int x1 = wrap2(cx + 1, g.nx), y1 = wrap2(cy + 1, g.ny);
+			e00 = a.E32[((int64_t) cy << g.lnx) + cx];
+			e01 = a.E32[((int64_t) y1 << g.lnx) + cx];
+			e10 = a.E32[((int64_t) cy << g.lnx) + x1];
+			e11 = a.E32[((int64_t) y1 << g.lnx) + x1];
 		}
 		float ex = w00 * e00.x + w01 * e01.x + w10 * e10.x + w11 * e11.x;
 		float ey = w00 * e00.y + w01 * e01.y + w10 * e10.y + w11 * e11.y;
@@ -304,7 +384,7 @@ struct Mix {
 		float vpy = vmy - vmx * sp.tz_f;
 		float ux = vmx + vpy * sp.sz_f + dtqm2 * ex;
 		float uy = vmy - vpx * sp.sz_f + dtqm2 * ey;
-		if(fabsf(ux) > (float) sp.umax_x || fabsf(uy) > (float) sp.umax_y)
+		if(fabsf(ux) > sp.umax_x_f || fabsf(uy) > sp.umax_y_f)
 			o.err |= ST_UMAX;
 		if(!isfinite(ux) || !isfinite(uy))
 		{
@@ -322,16 +402,15 @@ struct Mix {
 			if(ox >= 1.0f) { ox -= 1.0f; sx += 1; }
 			if(oy >= 1.0f) { oy -= 1.0f; sy += 1; }
 		}
-		int ncx = wrapi(cx + sx, g.nx), ncy = wrapi(cy + sy, g.ny);
-		r.cell = ncy * g.nx + ncx;
+		int ncx = wrap2(cx + sx, g.nx), ncy = wrap2(cy + sy, g.ny);
+		r.cell = (ncy << g.lnx) + ncx;
 		r.ox = ox; r.oy = oy; r.ux = ux; r.uy = uy;
 
 		dxo = 1.0f - ox; dyo = 1.0f - oy;
-		float q = sp.qfix_f;
-		o.w[0] = (long long) __float2int_rn(dxo * dyo * q);
-		o.w[1] = (long long) __float2int_rn(dxo * oy * q);
-		o.w[2] = (long long) __float2int_rn(ox * dyo * q);
-		o.w[3] = (long long) __float2int_rn(ox * oy * q);
+		o.wq[0] = wfix(dxo * dyo);
+		o.wq[1] = wfix(dxo * oy);
+		o.wq[2] = wfix(ox * dyo);
+		o.wq[3] = wfix(ox * oy);
 		o.dest = tile_of(g, ncx, ncy);
 		if(Etile)
 		{
@@ -346,13 +425,94 @@ struct Mix {
 		return o;
 	}
 
-	static __device__ __forceinline__ void dep_quirk(const PushArgs &, const Out &) {}
-
-	static __device__ __forceinline__ int cell_of(const Rec &r, const Grid &g, int &cx, int &cy)
+	// Shared layout, every array on its natural alignment (W is odd, so
+	// the 8-byte arrays come first): [u64 shadow W*W][float2 E tile
+	// (T+1)^2][u32 accumulator W*W].
+	static __device__ __forceinline__ unsigned long long *sh64(unsigned char *sm)
 	{
-		cx = r.cell % g.nx;
-		cy = r.cell / g.nx;
-		return 0;
+		return reinterpret_cast<unsigned long long *>(sm);
+	}
+	static __device__ __forceinline__ float2 *shE(unsigned char *sm, int W)
+	{
+		return reinterpret_cast<float2 *>(sm + (size_t) W * W * 8);
+	}
+	static __device__ __forceinline__ uint32_t *sh32(unsigned char *sm, int W, int T)
+	{
+		return reinterpret_cast<uint32_t *>(sm + (size_t) W * W * 8 + (size_t) (T + 1) * (T + 1) * 8);
+	}
+
+	static __device__ __forceinline__ void clear(unsigned char *sm, int W, int T)
+	{
+		uint32_t *a32 = sh32(sm, W, T);
+		unsigned long long *a64 = sh64(sm);
+		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+		{
+			a32[i] = 0;
+			a64[i] = 0;
+		}
+	}
+
+	// Move the 32-bit sums into the 64-bit shadow (between barriers).
+	static __device__ __forceinline__ void fold(unsigned char *sm, int W, int T)
+	{
+		uint32_t *a32 = sh32(sm, W, T);
+		unsigned long long *a64 = sh64(sm);
+		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+		{
+			a64[i] += a32[i];
+			a32[i] = 0;
+		}
+	}
+
+	static __device__ __forceinline__ void deposit(const PushArgs &a, int s, unsigned char *sm,
+			int W, int H, int tx0, int ty0, const Out &o)
+	{
+		int lx = o.rx + H, ly = o.ry + H;
+		if(sm && lx >= 0 && ly >= 0 && lx + 1 < W && ly + 1 < W)
+		{
+			uint32_t *p = sh32(sm, W, a.g.tx) + ly * W + lx;
+			atomicAdd(&p[0], o.wq[0]);
+			atomicAdd(&p[W], o.wq[1]);
+			atomicAdd(&p[1], o.wq[2]);
+			atomicAdd(&p[W + 1], o.wq[3]);
+		}
+		else
+		{
+			double sc = a.sp[s].wq_scale;
+			dep_global(a.rho, a.g, tx0 + o.rx, ty0 + o.ry,
+					__double2ll_rn((double) o.wq[0] * sc), __double2ll_rn((double) o.wq[1] * sc),
+					__double2ll_rn((double) o.wq[2] * sc), __double2ll_rn((double) o.wq[3] * sc));
+		}
+	}
+
+	static __device__ __forceinline__ void flush(const PushArgs &a, int s, unsigned char *sm,
+			int W, int H, int tx0, int ty0)
+	{
+		const uint32_t *a32 = sh32(sm, W, a.g.tx);
+		const unsigned long long *a64 = sh64(sm);
+		double sc = a.sp[s].wq_scale;
+		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+		{
+			unsigned long long v = a64[i] + a32[i];
+			if(v != 0)
+				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)],
+						__double2ll_rn((double) v * sc));
+		}
+	}
+
+	static __device__ __forceinline__ const void *load_field(const PushArgs &a, unsigned char *sm,
+			int W, int T, int tx0, int ty0)
+	{
+		const Grid &g = a.g;
+		float2 *Et = shE(sm, W);
+		int WE = g.tx + 1;
+		for(int i = threadIdx.x; i < WE * (g.ty + 1); i += blockDim.x)
+		{
+			int lx = i % WE, ly = i / WE;
+			int gx = wrap2(tx0 + lx, g.nx), gy = wrap2(ty0 + ly, g.ny);
+			Et[i] = a.E32[((int64_t) gy << g.lnx) + gx];
+		}
+		return Et;
 	}
 
 	static __device__ __forceinline__ Rec from_spill(const Spill &S, int64_t k, const Grid &g)
@@ -360,11 +520,11 @@ struct Mix {
 		Rec r;
 		double px = S.x[k] * g.idx, py = S.y[k] * g.idy;
 		double fx = floor(px), fy = floor(py);
-		int cx = wrapi((int) fx, g.nx), cy = wrapi((int) fy, g.ny);
+		int cx = wrap2((int) fx, g.nx), cy = wrap2((int) fy, g.ny);
 		float ox = (float) (px - fx), oy = (float) (py - fy);
-		if(ox >= 1.0f) { ox = 0.0f; cx = wrapi(cx + 1, g.nx); }
-		if(oy >= 1.0f) { oy = 0.0f; cy = wrapi(cy + 1, g.ny); }
-		r.cell = cy * g.nx + cx;
+		if(ox >= 1.0f) { ox = 0.0f; cx = wrap2(cx + 1, g.nx); }
+		if(oy >= 1.0f) { oy = 0.0f; cy = wrap2(cy + 1, g.ny); }
+		r.cell = (cy << g.lnx) + cx;
 		r.ox = ox; r.oy = oy;
 		r.ux = (float) S.ux[k]; r.uy = (float) S.uy[k];
 		r.id = S.id[k];
@@ -374,58 +534,47 @@ struct Mix {
 	static __device__ __forceinline__ void to_spill_vals(const Rec &r, const Grid &g,
 			double &x, double &y, double &ux, double &uy)
 	{
-		int cx = r.cell % g.nx, cy = r.cell / g.nx;
+		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
 		x = ((double) cx + (double) r.ox) * g.dx;
 		y = ((double) cy + (double) r.oy) * g.dy;
 		ux = r.ux; uy = r.uy;
+	}
+
+	static __device__ __forceinline__ int cell_of(const Rec &r, const Grid &g, int &cx, int &cy)
+	{
+		cx = r.cell & (g.nx - 1);
+		cy = r.cell >> g.lnx;
+		return 0;
 	}
 };
 
 // ============================================================== kernels
 
-// One block per (tile, species).  Dynamic shared memory: the W x W
-// fixed-point accumulator (W = T + 2H + 1) followed, for the mixed form,
-// by the (TX+1) x (TY+1) E tile.
 template <class F>
-__global__ void __launch_bounds__(kPushThreads)
+__global__ void __launch_bounds__(kPushThreads, F::kMinBlocks)
 k_push(const PushArgs a)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
-	__shared__ int warp_tot[kPushThreads / 32];
+	__shared__ int s_cursor;
 	const Grid &g = a.g;
 	const int s = blockIdx.y;
 	const int t = blockIdx.x;
 	const Tiles &T = a.tiles[s];
 	const int H = g.halo;
 	const int W = g.tx + 2 * H + 1;
-	long long *acc = reinterpret_cast<long long *>(smem);
-	float2 *Et = reinterpret_cast<float2 *>(acc + W * W);
-	const int tx0 = (t % g.ntx) * g.tx, ty0 = (t / g.ntx) * g.ty;
+	const int tx0 = (t & (g.ntx - 1)) << g.ltx;
+	const int ty0 = (t >> (g.lnx - g.ltx)) << g.lty;
 
-	for(int i = threadIdx.x; i < W * W; i += blockDim.x)
-		acc[i] = 0;
-	const void *Etile = nullptr;
-	if(a.E32)
-	{
-		int WE = g.tx + 1;
-		for(int i = threadIdx.x; i < WE * (g.ty + 1); i += blockDim.x)
-		{
-			int lx = i % WE, ly = i / WE;
-			int gx = tx0 + lx, gy = ty0 + ly;
-			if(gx >= g.nx) gx -= g.nx;
-			if(gy >= g.ny) gy -= g.ny;
-			Et[i] = a.E32[(int64_t) gy * g.nx + gx];
-		}
-		Etile = Et;
-	}
+	F::clear(smem, W, g.tx);
+	const void *Etile = F::load_field(a, smem, W, g.tx, tx0, ty0);
+	if(threadIdx.x == 0) s_cursor = 0;
 	__syncthreads();
 
 	const int n = T.cnt[t];
 	const int64_t base = T.base[t];
-	int wptr = 0;
-	const unsigned lane_lt = (1u << (threadIdx.x & 31)) - 1;
+	const int lane = threadIdx.x & 31;
 
-	for(int c0 = 0; c0 < n; c0 += kChunk)
+	for(int c0 = 0, ci = 0; c0 < n; c0 += kChunk, ci++)
 	{
 		typename F::Rec rec[kPPT];
 		#pragma unroll
@@ -434,39 +583,41 @@ k_push(const PushArgs a)
 			int i = c0 + k * kPushThreads + threadIdx.x;
 			if(i < n) rec[k] = F::load(a, s, base + i);
 		}
-		// all loads of the chunk precede the in-place writes below
+		// every load of this chunk precedes the in-place writes below,
+		// and every deposit of the previous chunks precedes a fold
 		__syncthreads();
+		if(ci > 0 && ci % kFoldChunks == 0)
+		{
+			F::fold(smem, W, g.tx);
+			__syncthreads();
+		}
 		#pragma unroll
 		for(int k = 0; k < kPPT; k++)
 		{
 			int i = c0 + k * kPushThreads + threadIdx.x;
 			bool valid = i < n;
-			Out o;
+			typename F::Out o;
 			o.dest = t;
-			o.err = 0;
-			o.quirk = 0;
 			if(valid)
 			{
 				o = F::push(a, s, rec[k], tx0, ty0, Etile);
 				if(o.err) set_status(a.status, o.err);
-				if(o.quirk)
-					F::dep_quirk(a, o);
-				else
-					dep_tile(acc, W, H, g, tx0, ty0, o.rx, o.ry,
-							o.w[0], o.w[1], o.w[2], o.w[3], a.rho);
+				F::deposit(a, s, smem, W, H, tx0, ty0, o);
 			}
 			bool stay = valid && o.dest == t;
-			int tot;
-			int off = block_scan_flag(stay, warp_tot, &tot);
+			unsigned bs = __ballot_sync(0xffffffffu, stay);
+			int wb = 0;
+			if(lane == 0 && bs)
+				wb = atomicAdd(&s_cursor, __popc(bs));
+			wb = __shfl_sync(0xffffffffu, wb, 0);
 			if(stay)
-				F::store(a, s, base + wptr + off, rec[k]);
+				F::store(a, s, base + wb + __popc(bs & lanemask_lt()), rec[k]);
 			bool move = valid && o.dest != t;
-			unsigned movers = __ballot_sync(0xffffffffu, move);
+			int slot = warp_reserve(T.app, move, o.dest);
 			if(move)
 			{
-				int64_t slot = reserve_slot(a.tiles[s], o.dest, movers);
-				if(slot >= 0)
-					F::store(a, s, slot, rec[k]);
+				if(slot < T.cap[o.dest])
+					F::store(a, s, T.base[o.dest] + slot, rec[k]);
 				else
 				{
 					double x, y, ux, uy;
@@ -474,15 +625,12 @@ k_push(const PushArgs a)
 					spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id, a.status);
 				}
 			}
-			(void) lane_lt;
-			wptr += tot;
 		}
-		__syncthreads();
 	}
-	if(threadIdx.x == 0)
-		T.stay[t] = wptr;
 	__syncthreads();
-	flush_tile(acc, W, H, g, tx0, ty0, a.rho);
+	if(threadIdx.x == 0)
+		T.stay[t] = s_cursor;
+	F::flush(a, s, smem, W, H, tx0, ty0);
 }
 
 // Generic pass over the spill list: records with no tile of their own
@@ -506,24 +654,20 @@ k_spill(const SpillArgs sa)
 			int64_t k = k0 + threadIdx.x;
 			bool valid = k < ns;
 			typename F::Rec r;
-			Out o;
+			typename F::Out o;
 			o.dest = 0;
 			if(valid)
 			{
 				r = F::from_spill(S, k, g);
 				o = F::push(a, s, r, 0, 0, nullptr);
 				if(o.err) set_status(a.status, o.err);
-				if(o.quirk)
-					F::dep_quirk(a, o);
-				else
-					dep_global(a.rho, g, o.rx, o.ry, o.w[0], o.w[1], o.w[2], o.w[3]);
+				F::deposit(a, s, nullptr, 0, 0, 0, 0, o);
 			}
-			unsigned act = __ballot_sync(0xffffffffu, valid);
+			int slot = warp_reserve(a.tiles[s].app, valid, o.dest);
 			if(valid)
 			{
-				int64_t slot = reserve_slot(a.tiles[s], o.dest, act);
-				if(slot >= 0)
-					F::store(a, s, slot, r);
+				if(slot < a.tiles[s].cap[o.dest])
+					F::store(a, s, a.tiles[s].base[o.dest] + slot, r);
 				else
 				{
 					double x, y, ux, uy;
