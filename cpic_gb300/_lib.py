@@ -16,6 +16,7 @@ MIXED = 1
 STATUS = {
     0: "CPIC_OK", -1: "CPIC_EINVAL", -2: "CPIC_ENOMEM", -3: "CPIC_ECUDA", -4: "CPIC_EUMAX",
     -5: "CPIC_ENAN", -6: "CPIC_ECAPACITY", -7: "CPIC_EDONE", -8: "CPIC_ENODEV", -9: "CPIC_ESTATE",
+    -10: "CPIC_ETIMEOUT",
 }
 
 

@@ -25,8 +25,8 @@
 namespace cpic {
 
 constexpr int kMaxSpecies = 8;
-constexpr int kPushThreads = 256;
-constexpr int kPPT = 4;                       // particles per thread per chunk
+constexpr int kPushThreads = 512;
+constexpr int kPPT = 2;                       // particles per thread per chunk
 constexpr int kChunk = kPushThreads * kPPT;   // particles per chunk
 constexpr int kWeightBits = 20;
 constexpr int kFoldChunks = 2;   // kFoldChunks * kChunk * 2^kWeightBits <= 2^31
@@ -37,6 +37,7 @@ enum : uint32_t {
 	ST_NAN = 1u << 1,        // non-finite particle state
 	ST_SPILL_FULL = 1u << 2, // spill list full: particles would be lost
 	ST_RANGE = 1u << 3,      // a cell index outside the grid (defensive)
+	ST_TIMEOUT = 1u << 4,    // a bounded wait on a bulk copy expired
 };
 
 struct StoreF64 {
@@ -187,6 +188,70 @@ warp_reserve(int32_t *app, bool move, int dest)
 		pending &= ~grp;
 	}
 	return slot;
+}
+
+// ------------------------------------------------ bulk copies (TMA engine)
+//
+// One thread streams a chunk of each structure-of-arrays column from global
+// into shared memory with cp.async.bulk; completion is counted in bytes on
+// an mbarrier that every consumer thread waits on.
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+	return (uint32_t) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Order this thread's earlier generic-proxy accesses to shared memory
+// before later async-proxy (bulk copy) writes to it.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+			:: "r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// dst (shared) and src (global) 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+			:: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\t"
+			"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+	return ok != 0;
+}
+
+// Wait for the mbarrier phase of the given parity, with an iteration limit:
+// on expiry the status word records ST_TIMEOUT and the caller goes on (its
+// indices are all clamped, so stale shared data cannot cause an
+// out-of-bounds access).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *status)
+{
+	for(uint32_t it = 0; it < (1u << 22); it++)
+		if(mbar_try_wait(bar, parity))
+			return true;
+	set_status(status, ST_TIMEOUT);
+	return false;
 }
 
 // Append a record to a spill list; false when the list is full.

@@ -394,10 +394,12 @@ static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
 
 static size_t push_smem(const cpic_ctx *c)
 {
+	// two staged chunks plus the form's accumulators and field tile
 	int W = c->g.tx + 2 * c->g.halo + 1;
+	// (+128: the kernel rounds the dynamic base up to 128 bytes)
 	if(c->precision == CPIC_MIXED)
-		return Mix::smem_bytes(W, c->g.tx);
-	return F64::smem_bytes(W, c->g.tx);
+		return 128 + 2 * Mix::stage_bytes(c->p.track_ids != 0) + Mix::smem_bytes(W, c->g.tx);
+	return 128 + 2 * F64::stage_bytes(true) + F64::smem_bytes(W, c->g.tx);
 }
 
 static int check_status(cpic_ctx *c)
@@ -409,6 +411,7 @@ static int check_status(cpic_ctx *c)
 	if(st & ST_UMAX) return CPIC_EUMAX;
 	if(st & ST_NAN) return CPIC_ENAN;
 	if(st & ST_RANGE) return CPIC_EINVAL;
+	if(st & ST_TIMEOUT) return CPIC_ETIMEOUT;
 	return CPIC_OK;
 }
 

@@ -32,7 +32,7 @@ namespace cpic {
 
 struct F64 {
 	struct Rec { double x, y, ux, uy; int32_t id; };
-	static constexpr int kMinBlocks = 2;
+	static constexpr int kMinBlocks = 1;
 
 	struct Out {
 		int dest;        // destination tile
@@ -63,6 +63,36 @@ struct F64 {
 		const StoreF64 &st = a.f64[s];
 		st.x[i] = r.x; st.y[i] = r.y; st.ux[i] = r.ux; st.uy[i] = r.uy;
 		st.id[i] = r.id;
+	}
+
+	// Staged chunk layout: x, y, ux, uy (kChunk doubles each), id.
+	static __host__ __device__ __forceinline__ size_t stage_bytes(bool)
+	{
+		return (size_t) kChunk * (4 * sizeof(double) + sizeof(int32_t));
+	}
+
+	// Thread 0: arm `bar` and copy particles [c0, c0 + cnt) of the tile.
+	static __device__ __forceinline__ void stage_issue(const PushArgs &a, int s, int64_t first,
+			int cnt, unsigned char *buf, uint64_t *bar)
+	{
+		const StoreF64 &st = a.f64[s];
+		uint32_t b8 = (uint32_t) ((cnt * 8 + 15) & ~15);
+		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
+		mbar_arrive_expect_tx(bar, 4 * b8 + b4);
+		bulk_g2s(buf, st.x + first, b8, bar);
+		bulk_g2s(buf + kChunk * 8, st.y + first, b8, bar);
+		bulk_g2s(buf + kChunk * 16, st.ux + first, b8, bar);
+		bulk_g2s(buf + kChunk * 24, st.uy + first, b8, bar);
+		bulk_g2s(buf + kChunk * 32, st.id + first, b4, bar);
+	}
+
+	static __device__ __forceinline__ Rec from_stage(const unsigned char *buf, int j, bool)
+	{
+		const double *d = reinterpret_cast<const double *>(buf);
+		Rec r;
+		r.x = d[j]; r.y = d[kChunk + j]; r.ux = d[2 * kChunk + j]; r.uy = d[3 * kChunk + j];
+		r.id = reinterpret_cast<const int32_t *>(buf + kChunk * 32)[j];
+		return r;
 	}
 
 	// relative_position_grid, interpolate.c:38-66 (field origin 0 on one
@@ -292,7 +322,7 @@ struct F64 {
 
 struct Mix {
 	struct Rec { int32_t cell; float ox, oy, ux, uy; int32_t id; };
-	static constexpr int kMinBlocks = 4;
+	static constexpr int kMinBlocks = 2;
 
 	struct Out {
 		int dest;
@@ -327,6 +357,39 @@ struct Mix {
 		st.ox[i] = r.ox; st.oy[i] = r.oy;
 		st.ux[i] = r.ux; st.uy[i] = r.uy;
 		if(st.id) st.id[i] = r.id;
+	}
+
+	// Staged chunk layout: cell, ox, oy, ux, uy (kChunk 32-bit words
+	// each) and, when ids are tracked, id.
+	static __host__ __device__ __forceinline__ size_t stage_bytes(bool ids)
+	{
+		return (size_t) kChunk * 4 * (ids ? 6 : 5);
+	}
+
+	static __device__ __forceinline__ void stage_issue(const PushArgs &a, int s, int64_t first,
+			int cnt, unsigned char *buf, uint64_t *bar)
+	{
+		const StoreMix &st = a.mix[s];
+		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
+		mbar_arrive_expect_tx(bar, (st.id ? 6 : 5) * b4);
+		bulk_g2s(buf, st.cell + first, b4, bar);
+		bulk_g2s(buf + kChunk * 4, st.ox + first, b4, bar);
+		bulk_g2s(buf + kChunk * 8, st.oy + first, b4, bar);
+		bulk_g2s(buf + kChunk * 12, st.ux + first, b4, bar);
+		bulk_g2s(buf + kChunk * 16, st.uy + first, b4, bar);
+		if(st.id)
+			bulk_g2s(buf + kChunk * 20, st.id + first, b4, bar);
+	}
+
+	static __device__ __forceinline__ Rec from_stage(const unsigned char *buf, int j, bool ids)
+	{
+		const float *f = reinterpret_cast<const float *>(buf);
+		Rec r;
+		r.cell = reinterpret_cast<const int32_t *>(buf)[j];
+		r.ox = f[kChunk + j]; r.oy = f[2 * kChunk + j];
+		r.ux = f[3 * kChunk + j]; r.uy = f[4 * kChunk + j];
+		r.id = ids ? reinterpret_cast<const int32_t *>(buf)[5 * kChunk + j] : 0;
+		return r;
 	}
 
 	// round(w * 2^kWeightBits) for w in [0, 1]: adding 2^23 puts the
@@ -554,7 +617,9 @@ template <class F>
 __global__ void __launch_bounds__(kPushThreads, F::kMinBlocks)
 k_push(const PushArgs a)
 {
-	extern __shared__ __align__(16) unsigned char smem[];
+	// dynamic shared memory: two staged chunks, then the form's area
+	extern __shared__ __align__(128) unsigned char smem[];
+	__shared__ __align__(8) uint64_t bars[2];
 	__shared__ int s_cursor;
 	const Grid &g = a.g;
 	const int s = blockIdx.y;
@@ -564,45 +629,66 @@ k_push(const PushArgs a)
 	const int W = g.tx + 2 * H + 1;
 	const int tx0 = (t & (g.ntx - 1)) << g.ltx;
 	const int ty0 = (t >> (g.lnx - g.ltx)) << g.lty;
+	const bool ids = a.mix[s].id != nullptr;
+	const size_t sb = F::stage_bytes(ids);
+	// bulk-copy destinations need 16-byte alignment; the host adds 128
+	// bytes of slack for this round-up
+	unsigned char *stage0 = reinterpret_cast<unsigned char *>(
+			(reinterpret_cast<uintptr_t>(smem) + 127) & ~(uintptr_t) 127);
+	unsigned char *fsm = stage0 + 2 * sb;
 
-	F::clear(smem, W, g.tx);
-	const void *Etile = F::load_field(a, smem, W, g.tx, tx0, ty0);
-	if(threadIdx.x == 0) s_cursor = 0;
-	__syncthreads();
-
+	F::clear(fsm, W, g.tx);
+	const void *Etile = F::load_field(a, fsm, W, g.tx, tx0, ty0);
 	const int n = T.cnt[t];
 	const int64_t base = T.base[t];
+	const int nchunks = (n + kChunk - 1) / kChunk;
+	if(threadIdx.x == 0)
+	{
+		s_cursor = 0;
+		mbar_init(&bars[0], 1);
+		mbar_init(&bars[1], 1);
+		fence_mbar_init();
+	}
+	__syncthreads();
+	if(threadIdx.x == 0 && nchunks > 0)
+		F::stage_issue(a, s, base, min(kChunk, n), stage0, &bars[0]);
 	const int lane = threadIdx.x & 31;
 
-	for(int c0 = 0, ci = 0; c0 < n; c0 += kChunk, ci++)
+	for(int ci = 0; ci < nchunks; ci++)
 	{
-		typename F::Rec rec[kPPT];
-		#pragma unroll
-		for(int k = 0; k < kPPT; k++)
+		const int c0 = ci * kChunk;
+		// prefetch the next chunk into the other buffer, whose previous
+		// contents were consumed before the barrier ending the last pass
+		if(threadIdx.x == 0 && ci + 1 < nchunks)
 		{
-			int i = c0 + k * kPushThreads + threadIdx.x;
-			if(i < n) rec[k] = F::load(a, s, base + i);
+			fence_proxy_async_smem();
+			F::stage_issue(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
+					stage0 + ((ci + 1) & 1) * sb, &bars[(ci + 1) & 1]);
 		}
-		// every load of this chunk precedes the in-place writes below,
-		// and every deposit of the previous chunks precedes a fold
-		__syncthreads();
+		// this chunk has landed: every global read of slots below
+		// c0 + kChunk is complete, so the in-place writes below are safe
+		mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status);
 		if(ci > 0 && ci % kFoldChunks == 0)
 		{
-			F::fold(smem, W, g.tx);
+			// every deposit of the previous chunks precedes the fold
+			F::fold(fsm, W, g.tx);
 			__syncthreads();
 		}
+		const unsigned char *buf = stage0 + (ci & 1) * sb;
 		#pragma unroll
 		for(int k = 0; k < kPPT; k++)
 		{
-			int i = c0 + k * kPushThreads + threadIdx.x;
-			bool valid = i < n;
+			const int j = k * kPushThreads + threadIdx.x;
+			bool valid = c0 + j < n;
+			typename F::Rec rec[1];
 			typename F::Out o;
 			o.dest = t;
 			if(valid)
 			{
-				o = F::push(a, s, rec[k], tx0, ty0, Etile);
+				rec[0] = F::from_stage(buf, j, ids);
+				o = F::push(a, s, rec[0], tx0, ty0, Etile);
 				if(o.err) set_status(a.status, o.err);
-				F::deposit(a, s, smem, W, H, tx0, ty0, o);
+				F::deposit(a, s, fsm, W, H, tx0, ty0, o);
 			}
 			bool stay = valid && o.dest == t;
 			unsigned bs = __ballot_sync(0xffffffffu, stay);
@@ -611,26 +697,27 @@ k_push(const PushArgs a)
 				wb = atomicAdd(&s_cursor, __popc(bs));
 			wb = __shfl_sync(0xffffffffu, wb, 0);
 			if(stay)
-				F::store(a, s, base + wb + __popc(bs & lanemask_lt()), rec[k]);
+				F::store(a, s, base + wb + __popc(bs & lanemask_lt()), rec[0]);
 			bool move = valid && o.dest != t;
 			int slot = warp_reserve(T.app, move, o.dest);
 			if(move)
 			{
 				if(slot < T.cap[o.dest])
-					F::store(a, s, T.base[o.dest] + slot, rec[k]);
+					F::store(a, s, T.base[o.dest] + slot, rec[0]);
 				else
 				{
 					double x, y, ux, uy;
-					F::to_spill_vals(rec[k], g, x, y, ux, uy);
-					spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id, a.status);
+					F::to_spill_vals(rec[0], g, x, y, ux, uy);
+					spill_push(a.spill_out[s], x, y, ux, uy, rec[0].id, a.status);
 				}
 			}
 		}
+		// every read of this buffer precedes its refill
+		__syncthreads();
 	}
-	__syncthreads();
 	if(threadIdx.x == 0)
 		T.stay[t] = s_cursor;
-	F::flush(a, s, smem, W, H, tx0, ty0);
+	F::flush(a, s, fsm, W, H, tx0, ty0);
 }
 
 // Generic pass over the spill list: records with no tile of their own

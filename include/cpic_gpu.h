@@ -46,6 +46,7 @@ enum cpic_status {
 	CPIC_EDONE = -7,      /* iter >= cycles (sim_step returns -1, sim.c:486) */
 	CPIC_ENODEV = -8,     /* no CUDA device */
 	CPIC_ESTATE = -9,     /* call out of order (e.g. step before pre_step) */
+	CPIC_ETIMEOUT = -10,  /* a bounded device-side wait expired */
 };
 
 /* Simulation parameters; the .conf key each field comes from is named.
