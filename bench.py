@@ -39,6 +39,9 @@ WORKLOADS = {
     "two_stream_2048": (2048, 100, 0.2, 0.01, 0.01,
                         "two-stream 2048x2048, 100 electrons/cell (419,430,400), beams +-0.2, "
                         "vth 0.01, amp 0.01, dt 0.05"),
+    "two_stream_1024": (1024, 100, 0.2, 0.01, 0.01,
+                        "two-stream 1024x1024, 100 electrons/cell (104,857,600), beams +-0.2, "
+                        "vth 0.01, amp 0.01, dt 0.05"),
     "two_stream_512": (512, 100, 0.2, 0.01, 0.01,
                        "two-stream 512x512, 100 electrons/cell (26,214,400), beams +-0.2, vth 0.01, "
                        "amp 0.01, dt 0.05"),
@@ -153,10 +156,13 @@ def make_state(grid, ppc, v0, vth, amp, seed=2024):
     return dict(n=n, L=L, q=q, m=-q, x=x, y=y, ux=ux, uy=uy)
 
 
+TILE = {"tile": 0, "halo": 0}
+
+
 def make_ctx(grid, st, precision, dt):
     from cpic_gb300 import _lib
     ctx = _lib.Context(grid, grid, st["L"], st["L"], dt, 1.0, (0.0, 0.0, 0.0), precision=precision,
-                       track_ids=False)
+                       track_ids=False, tile=TILE["tile"], halo=TILE["halo"])
     return ctx
 
 
@@ -373,7 +379,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tile", type=int, default=0, help="tile size in cells (0: library default)")
+    ap.add_argument("--halo", type=int, default=0, help="deposit halo in cells (0: library default)")
     args = ap.parse_args()
+    TILE["tile"], TILE["halo"] = args.tile, args.halo
     args.warmup = max(args.warmup, 0)
     ws, rank = dist()
     if ws > 1:

@@ -28,8 +28,8 @@ constexpr int kMaxSpecies = 8;
 constexpr int kPushThreads = 512;
 constexpr int kPPT = 2;                       // particles per thread per chunk
 constexpr int kChunk = kPushThreads * kPPT;   // particles per chunk
-constexpr int kWeightBits = 20;
-constexpr int kFoldChunks = 2;   // kFoldChunks * kChunk * 2^kWeightBits <= 2^31
+constexpr int kWeightBits = 18;
+constexpr int kFoldChunks = 8;   // kFoldChunks * kChunk * 2^kWeightBits <= 2^31
 
 // Device status bits (sticky until the host clears them).
 enum : uint32_t {
@@ -165,6 +165,41 @@ frame_node(const Grid &g, int W, int H, int tx0, int ty0, int i)
 	return ((int64_t) gy << g.lnx) + gx;
 }
 
+// Split-phase variant: `issue` fires one atomic per distinct destination
+// (the leader lane keeps the old value), `finish` broadcasts it; the
+// atomics' latency overlaps whatever runs in between.  Whole warp.
+struct Resv { int leader, rank, own; };
+
+__device__ __forceinline__ Resv
+warp_reserve_issue(int32_t *app, bool move, int dest)
+{
+	Resv r = {0, 0, 0};
+	unsigned pending = __ballot_sync(0xffffffffu, move);
+	int lane = threadIdx.x & 31;
+	while(pending)
+	{
+		int leader = __ffs(pending) - 1;
+		int d = __shfl_sync(0xffffffffu, dest, leader);
+		unsigned grp = __ballot_sync(0xffffffffu, move && dest == d);
+		if(lane == leader)
+			r.own = atomicAdd(&app[d], __popc(grp));
+		if(grp & (1u << lane))
+		{
+			r.leader = leader;
+			r.rank = __popc(grp & lanemask_lt());
+		}
+		pending &= ~grp;
+	}
+	return r;
+}
+
+__device__ __forceinline__ int
+warp_reserve_finish(const Resv &r, bool move)
+{
+	int first = __shfl_sync(0xffffffffu, r.own, r.leader);
+	return move ? first + r.rank : -1;
+}
+
 // Warp-aggregated slot reservation for movers: one atomic per distinct
 // destination tile in the warp.  Must be called by the whole warp; returns
 // the slot within the destination tile for lanes with `move`, else -1.
@@ -229,6 +264,11 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 {
 	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
 			:: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)

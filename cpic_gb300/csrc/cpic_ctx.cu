@@ -934,12 +934,13 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	r = rebuild_species(c, s, true, &stg, n);
 	free_spill(stg);
 	if(r) return r;
-	// halo: 1.5x the largest initial displacement per step, plus one
+	// halo: 1.2x the largest initial displacement per step, plus one
+	// (faster particles deposit through global memory: correct, slower)
 	double vmax = 0.0;
 	for(int k = 0; k < c->nspecies; k++) vmax = std::max(vmax, c->sp[k].vmax);
 	if(c->p.halo <= 0)
 	{
-		int H = (int) ceil(1.5 * vmax * c->p.dt * std::max(c->g.idx, c->g.idy)) + 1;
+		int H = (int) ceil(1.2 * vmax * c->p.dt * std::max(c->g.idx, c->g.idy)) + 1;
 		H = std::max(1, std::min(H, c->g.tx));
 		c->g.halo = H;
 	}

@@ -73,6 +73,8 @@ void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 	if(!init)
 	{
 		cudaFuncSetAttribute(k_push<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		cudaFuncSetAttribute(k_push<F64>, cudaFuncAttributePreferredSharedMemoryCarveout,
+				cudaSharedmemCarveoutMaxShared);
 		init = true;
 	}
 	dim3 grid(ntiles, a.nspecies);

@@ -74,6 +74,8 @@ void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 	if(!init)
 	{
 		cudaFuncSetAttribute(k_push<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+		cudaFuncSetAttribute(k_push<Mix>, cudaFuncAttributePreferredSharedMemoryCarveout,
+				cudaSharedmemCarveoutMaxShared);
 		init = true;
 	}
 	dim3 grid(ntiles, a.nspecies);

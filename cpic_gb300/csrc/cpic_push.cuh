@@ -620,6 +620,7 @@ k_push(const PushArgs a)
 	// dynamic shared memory: two staged chunks, then the form's area
 	extern __shared__ __align__(128) unsigned char smem[];
 	__shared__ __align__(8) uint64_t bars[2];
+	__shared__ __align__(8) uint64_t ebars[2];
 	__shared__ int s_cursor;
 	const Grid &g = a.g;
 	const int s = blockIdx.y;
@@ -645,8 +646,10 @@ k_push(const PushArgs a)
 	if(threadIdx.x == 0)
 	{
 		s_cursor = 0;
-		mbar_init(&bars[0], 1);
+		mbar_init(&bars[0], 1);          // "full": one arrival + bytes
 		mbar_init(&bars[1], 1);
+		mbar_init(&ebars[0], kPushThreads / 32);   // "empty": one per warp
+		mbar_init(&ebars[1], kPushThreads / 32);
 		fence_mbar_init();
 	}
 	__syncthreads();
@@ -657,64 +660,93 @@ k_push(const PushArgs a)
 	for(int ci = 0; ci < nchunks; ci++)
 	{
 		const int c0 = ci * kChunk;
-		// prefetch the next chunk into the other buffer, whose previous
-		// contents were consumed before the barrier ending the last pass
-		if(threadIdx.x == 0 && ci + 1 < nchunks)
-		{
-			fence_proxy_async_smem();
-			F::stage_issue(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
-					stage0 + ((ci + 1) & 1) * sb, &bars[(ci + 1) & 1]);
-		}
-		// this chunk has landed: every global read of slots below
-		// c0 + kChunk is complete, so the in-place writes below are safe
-		mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status);
 		if(ci > 0 && ci % kFoldChunks == 0)
 		{
-			// every deposit of the previous chunks precedes the fold
+			// every deposit of the previous chunks precedes the fold, and
+			// the fold precedes every later deposit
+			__syncthreads();
 			F::fold(fsm, W, g.tx);
 			__syncthreads();
 		}
+		// prefetch the next chunk into the other buffer once every warp
+		// has released it (its last reader was chunk ci - 1)
+		if(threadIdx.x == 0 && ci + 1 < nchunks)
+		{
+			const int b = (ci + 1) & 1;
+			if(ci >= 1)
+				mbar_wait_bounded(&ebars[b], ((ci - 1) >> 1) & 1, a.status);
+			fence_proxy_async_smem();
+			F::stage_issue(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
+					stage0 + b * sb, &bars[b]);
+		}
+		// this chunk has landed: every global read of slots below
+		// c0 + kChunk is complete, so the in-place writes below are safe
+		// (the stayer cursor never passes the end of the chunks read)
+		mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status);
 		const unsigned char *buf = stage0 + (ci & 1) * sb;
+		typename F::Rec rec[kPPT];
+		int dest[kPPT];
+		unsigned bs[kPPT];
+		Resv rv[kPPT];
+		uint32_t err = 0;
 		#pragma unroll
 		for(int k = 0; k < kPPT; k++)
 		{
 			const int j = k * kPushThreads + threadIdx.x;
-			bool valid = c0 + j < n;
-			typename F::Rec rec[1];
-			typename F::Out o;
-			o.dest = t;
+			const bool valid = c0 + j < n;
+			dest[k] = -1;
 			if(valid)
 			{
-				rec[0] = F::from_stage(buf, j, ids);
-				o = F::push(a, s, rec[0], tx0, ty0, Etile);
-				if(o.err) set_status(a.status, o.err);
+				rec[k] = F::from_stage(buf, j, ids);
+				typename F::Out o = F::push(a, s, rec[k], tx0, ty0, Etile);
+				err |= o.err;
 				F::deposit(a, s, fsm, W, H, tx0, ty0, o);
+				dest[k] = o.dest;
 			}
-			bool stay = valid && o.dest == t;
-			unsigned bs = __ballot_sync(0xffffffffu, stay);
-			int wb = 0;
-			if(lane == 0 && bs)
-				wb = atomicAdd(&s_cursor, __popc(bs));
-			wb = __shfl_sync(0xffffffffu, wb, 0);
-			if(stay)
-				F::store(a, s, base + wb + __popc(bs & lanemask_lt()), rec[0]);
-			bool move = valid && o.dest != t;
-			int slot = warp_reserve(T.app, move, o.dest);
+			bs[k] = __ballot_sync(0xffffffffu, dest[k] == t);
+			// slots in the destination tiles: atomics issued now, their
+			// results consumed after the stayer writes
+			rv[k] = warp_reserve_issue(T.app, dest[k] >= 0 && dest[k] != t, dest[k]);
+		}
+		// this warp is done with the staged chunk: release the buffer
+		__syncwarp();
+		if(lane == 0)
+			mbar_arrive(&ebars[ci & 1]);
+		if(err) set_status(a.status, err);
+		// one shared-cursor reservation per warp for all its stayers
+		int nst = 0;
+		#pragma unroll
+		for(int k = 0; k < kPPT; k++) nst += __popc(bs[k]);
+		int wb = 0;
+		if(lane == 0 && nst)
+			wb = atomicAdd(&s_cursor, nst);
+		wb = __shfl_sync(0xffffffffu, wb, 0);
+		#pragma unroll
+		for(int k = 0; k < kPPT; k++)
+		{
+			if(bs[k] & (1u << lane))
+				F::store(a, s, base + wb + __popc(bs[k] & lanemask_lt()), rec[k]);
+			wb += __popc(bs[k]);
+		}
+		#pragma unroll
+		for(int k = 0; k < kPPT; k++)
+		{
+			const bool move = dest[k] >= 0 && dest[k] != t;
+			const int slot = warp_reserve_finish(rv[k], move);
 			if(move)
 			{
-				if(slot < T.cap[o.dest])
-					F::store(a, s, T.base[o.dest] + slot, rec[0]);
+				if(slot < T.cap[dest[k]])
+					F::store(a, s, T.base[dest[k]] + slot, rec[k]);
 				else
 				{
 					double x, y, ux, uy;
-					F::to_spill_vals(rec[0], g, x, y, ux, uy);
-					spill_push(a.spill_out[s], x, y, ux, uy, rec[0].id, a.status);
+					F::to_spill_vals(rec[k], g, x, y, ux, uy);
+					spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id, a.status);
 				}
 			}
 		}
-		// every read of this buffer precedes its refill
-		__syncthreads();
 	}
+	__syncthreads();
 	if(threadIdx.x == 0)
 		T.stay[t] = s_cursor;
 	F::flush(a, s, fsm, W, H, tx0, ty0);
