@@ -25,11 +25,21 @@
 namespace cpic {
 
 constexpr int kMaxSpecies = 8;
-constexpr int kPushThreads = 512;
-constexpr int kPPT = 2;                       // particles per thread per chunk
+// Block shape of the fused particle kernel (build-time knobs).
+#ifndef CPIC_PUSH_THREADS
+#define CPIC_PUSH_THREADS 256
+#endif
+#ifndef CPIC_PPT
+#define CPIC_PPT 2
+#endif
+constexpr int kPushThreads = CPIC_PUSH_THREADS;
+constexpr int kPPT = CPIC_PPT;                // particles per thread per chunk
 constexpr int kChunk = kPushThreads * kPPT;   // particles per chunk
 constexpr int kWeightBits = 18;
-constexpr int kFoldChunks = 8;   // kFoldChunks * kChunk * 2^kWeightBits <= 2^31
+// folds keep every 32-bit weight sum below 2^31:
+// kFoldChunks * kChunk * 2^kWeightBits <= 2^31
+constexpr int kFoldChunks = (1 << (31 - kWeightBits)) / kChunk;
+static_assert(kFoldChunks >= 1, "chunk too large for 32-bit weight sums");
 
 // Device status bits (sticky until the host clears them).
 enum : uint32_t {

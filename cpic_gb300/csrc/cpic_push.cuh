@@ -322,7 +322,7 @@ struct F64 {
 
 struct Mix {
 	struct Rec { int32_t cell; float ox, oy, ux, uy; int32_t id; };
-	static constexpr int kMinBlocks = 2;
+	static constexpr int kMinBlocks = kPushThreads >= 1024 ? 1 : 1024 / kPushThreads;
 
 	struct Out {
 		int dest;
