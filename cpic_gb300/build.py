@@ -26,7 +26,7 @@ UNITS = [
     ("cpic_fp64.cu", ["--fmad=false"]),
     ("cpic_mixed.cu", ["--fmad=true"]),
 ]
-C_UNITS = ["cpic_init.c"]
+C_UNITS = ["cpic_init.c", "cpic_conf.c"]
 
 
 def _nvcc():

@@ -1,0 +1,111 @@
+"""Build the reference (rodarima/cpic) from its own sources, in place,
+against the project-written shims, into oracle/_ref/ (git-ignored).
+
+TEST INFRASTRUCTURE ONLY.  Two variants:
+  shipped: src/*.c as they are (keeps the AVX2 lane-conflict loss of the
+           charge deposit, src/simd_avx2.h:392-410);
+  exact:   the same files through a symlink farm whose simd_avx2.h adds
+           colliding lanes one by one (oracle/exact/simd_avx2.h).
+Each variant yields ref_harness_<variant> (oracle/ref_harness.c) and the
+reference's own tests test_constant_speed_<variant>,
+test_cyclotron_<variant> (test/*.c), which read conf/*.conf relative to
+the reference tree.
+
+The reference needs MPI, FFTW3-MPI, libconfig, OmpSs-2/nanos6 and HDF5,
+none of which exist here: mpi.h, fftw3*.h, nanos6/debug.h and hdf5.h come
+from oracle/shims, libconfig.h from include/ with this project's parser
+(cpic_gb300/csrc/cpic_conf.c).  The MFT_TAP backend (mft_tap.c, tap.c,
+mft_worker.c) and the plotter are left out; cpic.c is left out because the
+harness and the tests bring their own main.  x86-64 only (AVX2
+intrinsics).  The reference tree is read, never written.
+"""
+import concurrent.futures as cf
+import os
+import platform
+import subprocess
+import sys
+
+REF = "/root/reference"
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_ref")
+SOURCES = ["sim", "field", "particle", "mover", "interpolate", "comm_plasma", "comm_field", "plist",
+           "mat", "plasma", "specie", "config", "perf", "utils", "solver", "output", "boundary"]
+CFLAGS = ["-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-DNDEBUG", "-DUSE_VECTOR_256",
+          "-march=core-avx2", "-Wno-unknown-pragmas", "-w"]
+
+
+def _run(cmd, cwd=None):
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=cwd)
+    if r.returncode != 0:
+        raise RuntimeError("%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def _farm(variant):
+    """Directory holding the variant's src view (symlinks only)."""
+    if variant == "shipped":
+        return os.path.join(REF, "src")
+    d = os.path.join(OUT, "exact_src")
+    os.makedirs(d, exist_ok=True)
+    for f in os.listdir(os.path.join(REF, "src")):
+        if not (f.endswith(".c") or f.endswith(".h")):
+            continue
+        dst = os.path.join(d, f)
+        src = os.path.join(HERE, "exact", f) if f == "simd_avx2.h" else os.path.join(REF, "src", f)
+        if os.path.islink(dst) or os.path.exists(dst):
+            os.remove(dst)
+        os.symlink(src, dst)
+    return d
+
+
+def build(force=False):
+    if not os.path.isdir(REF):
+        return None
+    if platform.machine() not in ("x86_64", "AMD64"):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    stamp = os.path.join(OUT, "built.txt")
+    if os.path.exists(stamp) and not force:
+        return OUT
+    inc = ["-I", os.path.join(HERE, "shims"), "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(REF, "include")]
+    jobs = []
+    common_objs = []
+    o = os.path.join(OUT, "shim_runtime.o")
+    jobs.append(["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-I", os.path.join(HERE, "shims"),
+                 "-c", os.path.join(HERE, "shims", "shim_runtime.c"), "-o", o])
+    common_objs.append(o)
+    o = os.path.join(OUT, "cpic_conf.o")
+    jobs.append(["gcc", "-std=gnu11", "-O2", "-c", os.path.join(ROOT, "cpic_gb300", "csrc", "cpic_conf.c"),
+                 "-o", o])
+    common_objs.append(o)
+    variant_objs = {}
+    for v in ("shipped", "exact"):
+        src = _farm(v)
+        extra = ['-DORC_REF_SIMD_AVX2="%s"' % os.path.join(REF, "src", "simd_avx2.h")] if v == "exact" else []
+        vinc = ["-iquote", src] + inc
+        objs = []
+        for s in SOURCES:
+            o = os.path.join(OUT, "%s_%s.o" % (v, s))
+            jobs.append(["gcc"] + CFLAGS + extra + vinc + ["-c", os.path.join(src, s + ".c"), "-o", o])
+            objs.append(o)
+        for name, path in (("harness", os.path.join(HERE, "ref_harness.c")),
+                           ("t_cs", os.path.join(REF, "test", "constant-speed.c")),
+                           ("t_cy", os.path.join(REF, "test", "cyclotron.c"))):
+            o = os.path.join(OUT, "%s_%s.o" % (v, name))
+            jobs.append(["gcc"] + CFLAGS + extra + ["-I", src] + inc + ["-c", path, "-o", o])
+        variant_objs[v] = objs
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        list(ex.map(_run, jobs))
+    for v, objs in variant_objs.items():
+        for name, exe in (("harness", "ref_harness_%s" % v), ("t_cs", "test_constant_speed_%s" % v),
+                          ("t_cy", "test_cyclotron_%s" % v)):
+            _run(["gcc", "-o", os.path.join(OUT, exe), os.path.join(OUT, "%s_%s.o" % (v, name))]
+                 + objs + common_objs + ["-lm", "-lpthread"])
+    with open(stamp, "w") as f:
+        f.write("reference built from %s/src with oracle shims\n" % REF)
+    return OUT
+
+
+if __name__ == "__main__":
+    print(build(force="-f" in sys.argv))

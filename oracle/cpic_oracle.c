@@ -66,110 +66,33 @@ typedef struct {
 
 /* ------------------------------------------------------------------ FFT */
 
-/* In-place iterative radix-2 complex FFT (sign = -1 forward, +1 inverse,
- * unnormalised); n must be a power of two.  Falls back to a direct DFT for
- * other n. */
-static void
-fft1(double *re, double *im, int64_t n, int sign)
-{
-	int64_t i, j, k, len;
-	if(n <= 1) return;
-	if(n & (n - 1))
-	{
-		double *tr = malloc(sizeof(double) * (size_t) n);
-		double *ti = malloc(sizeof(double) * (size_t) n);
-		for(k = 0; k < n; k++)
-		{
-			double sr = 0.0, si = 0.0;
-			for(j = 0; j < n; j++)
-			{
-				double a = sign * 2.0 * M_PI * (double) ((k * j) % n) / (double) n;
-				double c = cos(a), s = sin(a);
-				sr += re[j] * c - im[j] * s;
-				si += re[j] * s + im[j] * c;
-			}
-			tr[k] = sr; ti[k] = si;
-		}
-		memcpy(re, tr, sizeof(double) * (size_t) n);
-		memcpy(im, ti, sizeof(double) * (size_t) n);
-		free(tr); free(ti);
-		return;
-	}
-	for(i = 1, j = 0; i < n; i++)
-	{
-		int64_t bit = n >> 1;
-		for(; j & bit; bit >>= 1) j ^= bit;
-		j ^= bit;
-		if(i < j)
-		{
-			double t = re[i]; re[i] = re[j]; re[j] = t;
-			t = im[i]; im[i] = im[j]; im[j] = t;
-		}
-	}
-	for(len = 2; len <= n; len <<= 1)
-	{
-		int64_t half = len >> 1;
-		for(k = 0; k < half; k++)
-		{
-			double a = sign * 2.0 * M_PI * (double) k / (double) len;
-			double wr = cos(a), wi = sin(a);
-			for(i = k; i < n; i += len)
-			{
-				int64_t p = i + half;
-				double xr = re[p] * wr - im[p] * wi;
-				double xi = re[p] * wi + im[p] * wr;
-				re[p] = re[i] - xr; im[p] = im[i] - xi;
-				re[i] = re[i] + xr; im[i] = im[i] + xi;
-			}
-		}
-	}
-}
+#include "orc_fft.h"
 
-/* MFT Poisson solve, solver.c:466-509 (MFT_solve): r2c FFT of rho (rows
- * y, columns x, FFTW's n0 = ny, n1 = nx, solver.c:314-330), multiply by G
- * (MFT_kernel, solver.c:338-363), c2r, divide by nx*ny (MFT_normalize,
- * solver.c:366-379).  rho and phi use row stride `stride`. */
+/* MFT Poisson solve, solver.c:465-509 (MFT_solve): r2c FFT of rho (rows
+ * y, columns x: FFTW's n0 = ny, n1 = nx, solver.c:314-330), multiply by G
+ * (MFT_kernel, solver.c:337-363, complex times real), c2r, divide by
+ * nx*ny (MFT_normalize, solver.c:365-379).  rho and phi use row strides
+ * rstride / pstride. */
 static void
 mft_solve(int64_t nx, int64_t ny, const double *G, const double *rho,
 		int64_t rstride, double *phi, int64_t pstride)
 {
-	int64_t ix, iy, nh = nx / 2 + 1;
+	int64_t i, ix, iy, nh = nx / 2 + 1;
 	double *sr = malloc(sizeof(double) * (size_t) (nh * ny));
 	double *si = malloc(sizeof(double) * (size_t) (nh * ny));
-	double *br = malloc(sizeof(double) * (size_t) (nx > ny ? nx : ny));
-	double *bi = malloc(sizeof(double) * (size_t) (nx > ny ? nx : ny));
-
-	for(iy = 0; iy < ny; iy++)
+	orc_rows_r2c(nx, ny, rho, rstride, sr, si);
+	orc_cols(nx, ny, sr, si, -1);
+	for(i = 0; i < nh * ny; i++)
 	{
-		for(ix = 0; ix < nx; ix++) { br[ix] = rho[iy * rstride + ix]; bi[ix] = 0.0; }
-		fft1(br, bi, nx, -1);
-		for(ix = 0; ix < nh; ix++) { sr[iy * nh + ix] = br[ix]; si[iy * nh + ix] = bi[ix]; }
+		sr[i] *= G[i];
+		si[i] *= G[i];
 	}
-	for(ix = 0; ix < nh; ix++)
-	{
-		for(iy = 0; iy < ny; iy++) { br[iy] = sr[iy * nh + ix]; bi[iy] = si[iy * nh + ix]; }
-		fft1(br, bi, ny, -1);
-		for(iy = 0; iy < ny; iy++)
-		{
-			/* g *= G (complex times real) */
-			br[iy] *= G[iy * nh + ix];
-			bi[iy] *= G[iy * nh + ix];
-		}
-		fft1(br, bi, ny, +1);
-		for(iy = 0; iy < ny; iy++) { sr[iy * nh + ix] = br[iy]; si[iy * nh + ix] = bi[iy]; }
-	}
+	orc_cols(nx, ny, sr, si, +1);
+	orc_rows_c2r(nx, ny, sr, si, phi, pstride);
 	for(iy = 0; iy < ny; iy++)
-	{
-		/* Rebuild the Hermitian half as c2r does: X[nx-k] = conj(X[k]) */
-		for(ix = 0; ix < nh; ix++) { br[ix] = sr[iy * nh + ix]; bi[ix] = si[iy * nh + ix]; }
-		bi[0] = 0.0;
-		if(nx % 2 == 0) bi[nx / 2] = 0.0;
-		for(ix = nh; ix < nx; ix++) { br[ix] = br[nx - ix]; bi[ix] = -bi[nx - ix]; }
-		fft1(br, bi, nx, +1);
 		for(ix = 0; ix < nx; ix++)
-			phi[iy * pstride + ix] = br[ix] / (double) (nx * ny);
-	}
-	free(sr); free(si); free(br); free(bi);
+			phi[iy * pstride + ix] /= (double) (nx * ny);
+	free(sr); free(si);
 }
 
 /* Green's function, solver.c:257-280 (MFT_init). */

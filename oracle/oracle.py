@@ -22,7 +22,8 @@ _LIB = None
 
 def build(force=False):
     """Compile the oracle with the reference's FP semantics (no contraction)."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    deps = [SRC, os.path.join(HERE, "orc_fft.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cmd = ["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",

@@ -32,6 +32,62 @@ def test_exports_every_declared_symbol(lib):
         assert hasattr(lib, s), s
 
 
+def test_exports_libconfig_subset(lib):
+    text = open(os.path.join(ROOT, "include", "libconfig.h")).read()
+    names = set(re.findall(r"\b(config_\w+)\s*\(", text))
+    assert len(names) >= 30
+    for s in names:
+        assert hasattr(lib, s), s
+
+
+def test_conf_parser_reads_reference_syntax(lib, tmp_path):
+    conf = tmp_path / "a.conf"
+    inc = tmp_path / "b.conf"
+    inc.write_text('extra = { k = 0x10L; }\n')
+    conf.write_text("""# comment
+species = ( { name = "e" "lectron"; particles = 3; charge = -1.0 },
+            { name = "ion"; particles = 4; charge = 1.0e+0 } );
+grid = { points = [64, 32] }   // trailing
+/* block
+   comment */
+simulation : { time_step = 5.0e-2; flag = true; space_length = [6.28, 3.14]; }
+@include "b.conf"
+""")
+
+    class C(ctypes.Structure):
+        _fields_ = [("pad", ctypes.c_char * 512)]
+    c = C()
+    lib.config_init(ctypes.byref(c))
+    assert lib.config_read_file(ctypes.byref(c), str(conf).encode()) == 1
+    v = ctypes.c_double()
+    lib.config_lookup.restype = ctypes.c_void_p
+    assert lib.config_lookup_float(ctypes.byref(c), b"simulation.time_step", ctypes.byref(v)) == 1
+    assert v.value == 5.0e-2
+    i = ctypes.c_int()
+    assert lib.config_lookup_int(ctypes.byref(c), b"grid.points.[1]", ctypes.byref(i)) == 1
+    assert i.value == 32
+    # an integer setting is not a float (no auto-conversion, as libconfig)
+    assert lib.config_lookup_float(ctypes.byref(c), b"grid.points.[0]", ctypes.byref(v)) == 0
+    ll = ctypes.c_longlong()
+    assert lib.config_lookup_int64(ctypes.byref(c), b"extra.k", ctypes.byref(ll)) == 1
+    assert ll.value == 16
+    s = ctypes.c_char_p()
+    assert lib.config_lookup_string(ctypes.byref(c), b"species.[0].name", ctypes.byref(s)) == 1
+    assert s.value == b"electron"
+    sp = lib.config_lookup(ctypes.byref(c), b"species")
+    lib.config_setting_length.argtypes = [ctypes.c_void_p]
+    assert lib.config_setting_length(sp) == 2
+    lib.config_destroy(ctypes.byref(c))
+    bad = tmp_path / "bad.conf"
+    bad.write_text("a = ;\n")
+    c2 = C()
+    lib.config_init(ctypes.byref(c2))
+    assert lib.config_read_file(ctypes.byref(c2), str(bad).encode()) == 0
+    lib.config_error_line.restype = ctypes.c_int
+    assert lib.config_error_line(ctypes.byref(c2)) == 1
+    lib.config_destroy(ctypes.byref(c2))
+
+
 def test_no_device_reports_enodev(lib):
     import torch
     if torch.cuda.is_available():
