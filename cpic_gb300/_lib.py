@@ -70,6 +70,8 @@ SIGNATURES = [
     ("cpic_status_bits", ctypes.c_uint32, [ctypes.c_void_p]),
     ("cpic_time_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, D, D, D]),
     ("cpic_tile_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
+    ("cpic_poisson_noalloc", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                            ctypes.c_int64, ctypes.c_void_p]),
     ("cpic_uniform", None, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64, D]),
     ("cpic_normal", None, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64, D]),
     ("cpic_init_two_stream", None, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int64,

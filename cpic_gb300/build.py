@@ -25,6 +25,7 @@ UNITS = [
     ("cpic_ctx.cu", ["--fmad=false"]),
     ("cpic_fp64.cu", ["--fmad=false"]),
     ("cpic_mixed.cu", ["--fmad=true"]),
+    ("cpic_noalloc.cu", ["--fmad=false"]),
 ]
 C_UNITS = ["cpic_init.c", "cpic_conf.c"]
 

@@ -175,6 +175,26 @@ CPIC_API int cpic_time_steps(cpic_ctx_t *ctx, int64_t nsteps, double *ms_total,
  * capacity slack in percent}. */
 CPIC_API int cpic_tile_info(const cpic_ctx_t *ctx, int32_t *out);
 
+/* --- solve without allocation ------------------------------------------ */
+
+/* Largest grid side accepted by cpic_poisson_noalloc: its scratch is one
+ * fixed array of about 2.1 MB held by every GPU that loads the library. */
+#define CPIC_NOALLOC_MAX_N 512
+
+/* No counterpart in the reference.  Periodic FP64 Poisson solve phi = IFFT(G
+ * FFT(rho)) / (nx ny) with the reference's Green's function, for callers that
+ * must not allocate device memory (a fixed memory budget or their own pool
+ * owning the device, or host threads on which cudaMalloc/cudaFree and their
+ * implicit synchronisation must not appear).  rho and phi are the caller's
+ * device buffers, ny x nx row-major doubles; nx and ny powers of two in
+ * [4, CPIC_NOALLOC_MAX_N] (larger grids are rejected with CPIC_EINVAL);
+ * stream is a cudaStream_t (NULL: the default stream); asynchronous.  The
+ * scratch lives in a static device array shared by all calls: the first call
+ * on each device looks up its address (make that first call before any
+ * stream capture), and calls that overlap on the GPU race on it. */
+CPIC_API int cpic_poisson_noalloc(const double *rho, double *phi, int64_t nx, int64_t ny,
+		void *stream);
+
 /* --- seeded initial states (host only; no GPU needed) ----------------- */
 
 /* The i-th uniform / normal draw of (seed, stream), i < n. */
