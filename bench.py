@@ -366,6 +366,67 @@ def run_reference(args):
             "wall_seconds": el}
 
 
+def _growth_rate(t, we):
+    """Least-squares slope of ln(W_E) / 2 (field amplitude growth rate)."""
+    t = np.asarray(t)
+    y = np.log(np.asarray(we))
+    A = np.vstack([t, np.ones_like(t)]).T
+    slope = np.linalg.lstsq(A, y, rcond=None)[0][0]
+    return 0.5 * slope
+
+
+def study_accuracy(args):
+    """Mixed form against the FP64 form on the same workload from the same
+    initial state: field-energy error through the linear phase (steps
+    0..linear_steps), growth rate of the field amplitude fitted in the linear
+    window, and the drift of the total energy (field + kinetic) over the
+    whole run."""
+    from cpic_gb300 import _lib, build
+    build.build()
+    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
+    dt = 0.05
+    st = make_state(grid, ppc, v0, vth, amp)
+    ctx = {}
+    for name, prec in (("fp64", _lib.FP64), ("mixed", _lib.MIXED)):
+        c = make_ctx(grid, st, prec, dt)
+        c.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
+        c.pre_step()
+        ctx[name] = c
+    series = {k: {"we": [], "tot": []} for k in ctx}
+    for k in range(args.study_steps):
+        for name, c in ctx.items():
+            c.step()
+            d = c.diag()
+            series[name]["we"].append(d["WE"])
+            series[name]["tot"].append(d["WE"] + d["KE"])
+    lin = min(args.accuracy_steps, args.study_steps)
+    we64 = np.array(series["fp64"]["we"])
+    wem = np.array(series["mixed"]["we"])
+    rel = np.abs(wem - we64) / we64
+    t = dt * np.arange(1, args.study_steps + 1)
+    win = slice(max(1, lin // 6), lin)
+    res = {"study": "accuracy", "workload": desc, "steps": args.study_steps, "linear_steps": lin,
+           "we_rel_err_max_linear": float(rel[:lin].max()),
+           "we_rel_err_max_all": float(rel.max()),
+           "growth_window_steps": [win.start + 1, win.stop]}
+    for name in ("fp64", "mixed"):
+        we = np.array(series[name]["we"])
+        tot = np.array(series[name]["tot"])
+        res["growth_rate_" + name] = float(_growth_rate(t[win], we[win]))
+        res["energy_drift_" + name] = float((tot[-1] - tot[0]) / tot[0])
+        res["we_final_" + name] = float(we[-1])
+        res["we_max_" + name] = float(we.max())
+    res["growth_rate_rel_err"] = abs(res["growth_rate_mixed"] - res["growth_rate_fp64"]) / abs(
+        res["growth_rate_fp64"])
+    every = max(1, args.study_steps // 50)
+    res["we_samples"] = {"step": list(range(1, args.study_steps + 1, every)),
+                         "fp64": [float(v) for v in we64[::every]],
+                         "mixed": [float(v) for v in wem[::every]]}
+    for c in ctx.values():
+        c.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -374,7 +435,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="two_stream_2048", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--accuracy-steps", type=int, default=20)
+    ap.add_argument("--accuracy-steps", type=int, default=300,
+                    help="steps of the mixed-vs-FP64 field-energy comparison (linear phase)")
+    ap.add_argument("--study", default="", choices=["", "accuracy"],
+                    help="accuracy: long mixed-vs-FP64 run (growth rate, energy drift), no timing")
+    ap.add_argument("--study-steps", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -391,7 +456,10 @@ def main():
         td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         if torch.cuda.is_available():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.study == "accuracy":
+        out = study_accuracy(args) if rank == 0 else None
+    else:
+        out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if rank == 0 and out is not None:
         print(json.dumps(out))
     if ws > 1:

@@ -130,6 +130,29 @@ def test_multistep_two_species_bz(lib):
     assert abs(g.diag()["Q"]) < 1e-9
 
 
+def test_two_species_full_size(lib):
+    """512x512, 16 electrons and 16 ions (mass ratio 100) per cell, Bz = 0.5:
+    8,388,608 particles.  Two stages bit-exact from identical fields, then
+    three full steps with field energy within 1e-10."""
+    case = cases.two_species()
+    g, o = prepared(case)
+    assert rel_max(g.rho(), o.rho()) <= RHO_TOL
+    for it in range(2):
+        _one_stage(g, o)
+        for s in range(2):
+            for a, b in zip(g.particles(s), o.particles(s)):
+                assert np.array_equal(a, b), (it, s)
+        assert rel_max(g.rho(), o.rho()) <= RHO_TOL
+        o.stage_field_E()
+    g.stage_field_E()
+    for k in range(3):
+        g.step()
+        o.step()
+        we_g, we_o = g.diag()["WE"], o.diag()["WE"]
+        assert abs(we_g - we_o) / we_o <= WE_TOL, k
+    assert np.array_equal(g.cell_counts(), o.cell_counts())
+
+
 def test_mixed_vs_fp64_energy(lib):
     case = cases.two_stream(n=64 * 64 * 32, steps=100)
     g64 = cases.make_gpu(case, precision=_lib.FP64)
