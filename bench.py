@@ -404,7 +404,16 @@ def study_accuracy(args):
     wem = np.array(series["mixed"]["we"])
     rel = np.abs(wem - we64) / we64
     t = dt * np.arange(1, args.study_steps + 1)
-    win = slice(max(1, lin // 6), lin)
+    # exponential phase of the FP64 run: from W_E rising above 10x its
+    # noise level (median over the first linear_steps) to 30% of its peak
+    base = float(np.median(we64[:lin]))
+    above = np.nonzero(we64 > 10.0 * base)[0]
+    top = np.nonzero(we64 >= 0.3 * we64.max())[0]
+    i0 = int(above[0]) if len(above) else lin // 6
+    i1 = int(top[0]) if len(top) else lin
+    if i1 - i0 < 20:
+        i0, i1 = max(1, lin // 6), lin
+    win = slice(i0, i1)
     res = {"study": "accuracy", "workload": desc, "steps": args.study_steps, "linear_steps": lin,
            "we_rel_err_max_linear": float(rel[:lin].max()),
            "we_rel_err_max_all": float(rel.max()),

@@ -96,6 +96,7 @@ struct SpeciesStep {
 	double tz, sz;       // Boris t and s for B along z (mover.c:45-51)
 	double umax_x, umax_y;
 	double qfix;         // fixed-point units per unit of w: -q/e0 * qscale
+	double qlo_mul;      // FP64 form: 2^m, the scale of the remainder word
 	double wq_scale;     // mixed: fixed-point units per integer weight unit
 	float dtqm2_f, tz_f, sz_f;
 	float umax_x_f, umax_y_f;
@@ -113,6 +114,7 @@ struct PushArgs {
 	StoreMix mix[kMaxSpecies];
 	Spill spill_out[kMaxSpecies];
 	long long *rho;      // ny x nx fixed-point accumulator
+	long long *rho_lo;   // FP64 form: remainder word, 2^m finer (else null)
 	const double *Ex64, *Ey64;     // (ny + 3) x nx, FP64 form
 	const float2 *E32;             // ny x nx (Ex, Ey) interleaved, mixed form
 	uint32_t *status;
@@ -164,6 +166,22 @@ dep_global(long long *rho, const Grid &g, int cx, int cy,
 	red_global(&rho[((int64_t) y1 << g.lnx) + x0], w01);
 	red_global(&rho[((int64_t) y0 << g.lnx) + x1], w10);
 	red_global(&rho[((int64_t) y1 << g.lnx) + x1], w11);
+}
+
+// Two-word variant of dep_global (FP64 form: high and remainder words).
+__device__ __forceinline__ void
+dep_global2(long long *rho, long long *rlo, const Grid &g, int cx, int cy,
+		const long long hi[4], const long long lo[4])
+{
+	int x0 = wrap2(cx, g.nx), y0 = wrap2(cy, g.ny);
+	int x1 = wrap2(x0 + 1, g.nx), y1 = wrap2(y0 + 1, g.ny);
+	int64_t n[4] = {((int64_t) y0 << g.lnx) + x0, ((int64_t) y1 << g.lnx) + x0,
+		((int64_t) y0 << g.lnx) + x1, ((int64_t) y1 << g.lnx) + x1};
+	for(int c = 0; c < 4; c++)
+	{
+		red_global(&rho[n[c]], hi[c]);
+		red_global(&rlo[n[c]], lo[c]);
+	}
 }
 
 // Global node index of shared accumulator entry i (frame origin t0 - H).
@@ -329,7 +347,7 @@ void launch_spill_f64(const SpillArgs &a, cudaStream_t s);
 void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s);
 void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
-		const double *cosy, double *phi, cudaStream_t s);
+		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo);
 
 void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);

@@ -51,12 +51,14 @@ struct cpic_ctx {
 	int64_t iter;
 	bool prepared;
 	double qscale, qinv;
+	double qlo_mul, qinv_lo;  // FP64 form: remainder-word scales
 	cudaStream_t stream;
 	int nspecies;
 	SpeciesHost sp[kMaxSpecies];
 	int spill_cur;
 	// fields
 	long long *rho;           // ny x nx fixed point
+	long long *rho_lo;        // FP64 form: remainder word (else null)
 	double *phi64, *Ex64, *Ey64;
 	float *phi32;
 	float2 *E32;
@@ -283,18 +285,32 @@ __global__ void k_rho_sum(int64_t n, const long long *rho, long long *sum)
 		atomicAdd((unsigned long long *) sum, (unsigned long long) sh[0]);
 }
 
-__global__ void k_rho_to_f64(int64_t n, const long long *rho, double qinv, double *out)
+// Fixed point -> FP64; rlo (FP64 form) adds the remainder word.
+__global__ void k_rho_to_f64(int64_t n, const long long *rho, double qinv, const long long *rlo,
+		double qinv_lo, double *out)
 {
 	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
 			i += (int64_t) gridDim.x * blockDim.x)
-		out[i] = (double) rho[i] * qinv;
+	{
+		double v = (double) rho[i] * qinv;
+		if(rlo) v += (double) rlo[i] * qinv_lo;
+		out[i] = v;
+	}
 }
 
-__global__ void k_f64_to_rho(int64_t n, const double *in, double qscale, long long *rho)
+// FP64 -> fixed point: high word and (FP64 form) the exact remainder at the
+// 2^m finer scale.
+__global__ void k_f64_to_rho(int64_t n, const double *in, double qscale, long long *rho,
+		double qlo_mul, long long *rlo)
 {
 	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
 			i += (int64_t) gridDim.x * blockDim.x)
-		rho[i] = __double2ll_rn(in[i] * qscale);
+	{
+		double v = in[i] * qscale;
+		long long hi = __double2ll_rn(v);
+		rho[i] = hi;
+		if(rlo) rlo[i] = __double2ll_rn((v - (double) hi) * qlo_mul);
+	}
 }
 
 __global__ void k_iota(int64_t n, int32_t *id)
@@ -351,6 +367,7 @@ static PushArgs make_args(cpic_ctx *c, int cur_spill)
 		a.spill_out[s] = c->sp[s].spill[cur_spill ^ 1];
 	}
 	a.rho = c->rho;
+	a.rho_lo = c->rho_lo;
 	a.Ex64 = c->Ex64;
 	a.Ey64 = c->Ey64;
 	a.E32 = c->precision == CPIC_MIXED ? c->E32 : nullptr;
@@ -383,6 +400,7 @@ static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
 		st.umax_y = c->g.ny * c->g.dy / p.dt;
 		double vq = -q / p.e0;
 		st.qfix = vq * c->qscale;
+		st.qlo_mul = c->qlo_mul;
 		st.wq_scale = st.qfix * ldexp(1.0, -kWeightBits);
 		st.dtqm2_f = (float) st.dtqm2;
 		st.tz_f = (float) st.tz;
@@ -632,6 +650,8 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 	cudaStream_t st = c->stream;
 	int64_t ng = (int64_t) c->g.nx * c->g.ny;
 	CK(cudaMemsetAsync(c->rho, 0, ng * sizeof(long long), st));
+	if(c->rho_lo)
+		CK(cudaMemsetAsync(c->rho_lo, 0, ng * sizeof(long long), st));
 	int cur = c->spill_cur;
 	for(int s = 0; s < c->nspecies; s++)
 		CK(cudaMemsetAsync(c->sp[s].spill[cur ^ 1].count, 0, sizeof(int32_t), st));
@@ -690,7 +710,7 @@ static int field_stage_async(cpic_ctx *c)
 	else
 	{
 		launch_poisson_f64(c->g, c->rho, c->qinv, c->spec64, c->twx64, c->twy64,
-				c->cosx, c->cosy, c->phi64, st);
+				c->cosx, c->cosy, c->phi64, st, c->rho_lo, c->qinv_lo);
 		launch_E_f64(c->g, c->phi64, c->Ex64, c->Ey64, st);
 	}
 	CK(cudaGetLastError());
@@ -789,6 +809,7 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	if(c->precision == CPIC_FP64)
 	{
 		AL(c->phi64, ng * sizeof(double));
+		AL(c->rho_lo, ng * sizeof(long long));
 		AL(c->Ex64, (ng + 3 * (int64_t) g.nx) * sizeof(double));
 		AL(c->Ey64, (ng + 3 * (int64_t) g.nx) * sizeof(double));
 		AL(c->spec64, ng / g.nx * nh * sizeof(double2));
@@ -808,6 +829,7 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	}
 #undef AL
 	cudaMemset(c->rho, 0, ng * sizeof(long long));
+	if(c->rho_lo) cudaMemset(c->rho_lo, 0, ng * sizeof(long long));
 	cudaMemset(c->status, 0, sizeof(uint32_t));
 	{
 		// Green's function cosines as MFT_init computes them
@@ -859,7 +881,7 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 		free_spill(S.spill[0]);
 		free_spill(S.spill[1]);
 	}
-	cudaFree(c->rho); cudaFree(c->phi64); cudaFree(c->Ex64); cudaFree(c->Ey64);
+	cudaFree(c->rho); cudaFree(c->rho_lo); cudaFree(c->phi64); cudaFree(c->Ex64); cudaFree(c->Ey64);
 	cudaFree(c->phi32); cudaFree(c->E32); cudaFree(c->spec64); cudaFree(c->spec32);
 	cudaFree(c->twx64); cudaFree(c->twy64); cudaFree(c->twx32); cudaFree(c->twy32);
 	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->mean); cudaFree(c->rho_sum);
@@ -880,6 +902,15 @@ static void update_qscale(cpic_ctx *c)
 	int k = (int) floor(62.0 - log2(bound)) - 1;
 	c->qscale = ldexp(1.0, k);
 	c->qinv = ldexp(1.0, -k);
+	// FP64 form: remainder word at 2^m finer resolution.  Every remainder
+	// is at most 2^(m-1) in magnitude and a node receives at most one per
+	// particle, so m = 62 - ceil(log2(N + 1)) keeps its sums below 2^62.
+	int64_t ntot = 0;
+	for(int s = 0; s < c->nspecies; s++) ntot += c->sp[s].n;
+	int m = 62 - (int) ceil(log2((double) ntot + 1.0));
+	if(m < 0) m = 0;
+	c->qlo_mul = ldexp(1.0, m);
+	c->qinv_lo = ldexp(1.0, -k - m);
 }
 
 CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
@@ -1104,7 +1135,8 @@ CPIC_API int cpic_get_rho(cpic_ctx_t *c, double *rho)
 	int64_t ng = (int64_t) c->g.nx * c->g.ny;
 	int r = ensure_scratch(c, ng);
 	if(r) return r;
-	k_rho_to_f64<<<grid_blocks(ng), 256, 0, c->stream>>>(ng, c->rho, c->qinv, c->scratch);
+	k_rho_to_f64<<<grid_blocks(ng), 256, 0, c->stream>>>(ng, c->rho, c->qinv, c->rho_lo,
+			c->qinv_lo, c->scratch);
 	CK(cudaMemcpyAsync(rho, c->scratch, ng * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
 	CK(cudaStreamSynchronize(c->stream));
 	return CPIC_OK;
@@ -1117,7 +1149,8 @@ CPIC_API int cpic_set_rho(cpic_ctx_t *c, const double *rho)
 	int r = ensure_scratch(c, ng);
 	if(r) return r;
 	CK(cudaMemcpyAsync(c->scratch, rho, ng * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-	k_f64_to_rho<<<grid_blocks(ng), 256, 0, c->stream>>>(ng, c->scratch, c->qscale, c->rho);
+	k_f64_to_rho<<<grid_blocks(ng), 256, 0, c->stream>>>(ng, c->scratch, c->qscale, c->rho,
+			c->qlo_mul, c->rho_lo);
 	CK(cudaStreamSynchronize(c->stream));
 	return CPIC_OK;
 }

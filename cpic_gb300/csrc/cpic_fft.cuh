@@ -77,9 +77,11 @@ __device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *
 // mode, removed in FP64 before the FP32 transform of the mixed form) comes
 // from the exact integer sum rsum; rsum null: no removal (FP64 form, as the
 // reference, whose G(0,0) = 0 discards the mode).
+// rho_lo (FP64 form, may be null): the remainder word at scale qinv_lo.
 template <typename T>
 __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, double qinv,
-		const long long *rsum, typename Cx<T>::t *spec, const typename Cx<T>::t *tw)
+		const long long *rsum, typename Cx<T>::t *spec, const typename Cx<T>::t *tw,
+		const long long *rho_lo, double qinv_lo)
 {
 	typedef typename Cx<T>::t C;
 	extern __shared__ unsigned char smem_raw[];
@@ -90,8 +92,14 @@ __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, dou
 	double m = rsum ? (double) *rsum * qinv / ((double) nx * (double) ny) : 0.0;
 	for(int i = threadIdx.x; i < nx; i += blockDim.x)
 	{
-		double va = (double) rho[(int64_t) r0 * nx + i] * qinv - m;
-		double vb = (double) rho[(int64_t) (r0 + 1) * nx + i] * qinv - m;
+		int64_t ia = (int64_t) r0 * nx + i, ib = (int64_t) (r0 + 1) * nx + i;
+		double va = (double) rho[ia] * qinv - m;
+		double vb = (double) rho[ib] * qinv - m;
+		if(rho_lo)
+		{
+			va += (double) rho_lo[ia] * qinv_lo;
+			vb += (double) rho_lo[ib] * qinv_lo;
+		}
 		C z; z.x = (T) va; z.y = (T) vb;
 		a[i] = z;
 	}
@@ -196,7 +204,8 @@ __global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<T>::t *
 template <typename T>
 static void poisson_launch(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		typename Cx<T>::t *spec, const typename Cx<T>::t *twx, const typename Cx<T>::t *twy,
-		const double *cosx, const double *cosy, T *phi, cudaStream_t s)
+		const double *cosx, const double *cosy, T *phi, cudaStream_t s,
+		const long long *rho_lo = nullptr, double qinv_lo = 0.0)
 {
 	typedef typename Cx<T>::t C;
 	int log2nx = 0, log2ny = 0;
@@ -204,7 +213,8 @@ static void poisson_launch(const Grid &g, const long long *rho, double qinv, con
 	while((1 << log2ny) < g.ny) log2ny++;
 	int rthreads = g.nx / 2 < 512 ? (g.nx / 2 < 32 ? 32 : g.nx / 2) : 512;
 	size_t rsm = 2 * (size_t) g.nx * sizeof(C);
-	k_rows_fwd<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, rho, qinv, mean, spec, twx);
+	k_rows_fwd<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, rho, qinv, mean, spec, twx,
+			rho_lo, qinv_lo);
 	int nh = g.nx / 2 + 1;
 	// columns per block: fill up to 128 KB of shared memory (two buffers)
 	int cb = (int) ((128 * 1024) / (2 * (size_t) g.ny * sizeof(C)));

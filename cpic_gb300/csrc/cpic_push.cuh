@@ -37,16 +37,17 @@ struct F64 {
 	struct Out {
 		int dest;        // destination tile
 		int rx, ry;      // new cell relative to the tile origin (unwrapped)
-		long long w[4];  // fixed-point deposit w00, w01, w10, w11
+		long long w[4];  // fixed-point deposit w00, w01, w10, w11 (high word)
+		long long wl[4]; // remainder words, 2^m finer
 		int quirk;       // position exactly on the upper boundary
 		int qx, qy;      // quirk: raw node indices
 		uint32_t err;
 	};
 
-	// shared memory: W x W 64-bit accumulator
+	// shared memory: W x W 64-bit high words, then W x W remainder words
 	static __host__ __device__ size_t smem_bytes(int W, int T)
 	{
-		return (size_t) W * W * sizeof(long long);
+		return 2 * (size_t) W * W * sizeof(long long);
 	}
 
 	static __device__ __forceinline__ Rec load(const PushArgs &a, int s, int64_t i)
@@ -207,10 +208,18 @@ struct F64 {
 		r.x = x; r.y = y; r.ux = ux; r.uy = uy;
 
 		// deposit weights of the new position (interpolate_p2f,
-		// interpolate.c:161-276), value w * (-q/e0) in fixed point
+		// interpolate.c:161-276), value w * (-q/e0) in two-word fixed
+		// point: c = w * qfix is the reference's addend scaled by 2^k
+		// (exactly: a power-of-two scale), hi its rounding, and the
+		// remainder c - hi (exact) is kept at 2^m finer resolution.
 		weights(g, x, y, w, i0x, i0y);
 		for(int c = 0; c < 4; c++)
-			o.w[c] = __double2ll_rn(w[c] * sp.qfix);
+		{
+			double v = w[c] * sp.qfix;
+			long long hi = __double2ll_rn(v);
+			o.w[c] = hi;
+			o.wl[c] = __double2ll_rn((v - (double) hi) * sp.qlo_mul);
+		}
 		if(i0x >= g.nx || i0y >= g.ny || i0x < 0 || i0y < 0)
 		{
 			// x == L or y == L after the wrap: keep the reference's
@@ -236,7 +245,7 @@ struct F64 {
 	static __device__ __forceinline__ void clear(unsigned char *sm, int W, int T)
 	{
 		long long *acc = reinterpret_cast<long long *>(sm);
-		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+		for(int i = threadIdx.x; i < 2 * W * W; i += blockDim.x)
 			acc[i] = 0;
 	}
 
@@ -263,6 +272,7 @@ struct F64 {
 				if(x < 0 || x >= g.nx || y < 0 || y > g.ny) continue;
 				if(y == g.ny) y = 0;
 				red_global(&a.rho[((int64_t) y << g.lnx) + x], o.w[c]);
+				red_global(&a.rho_lo[((int64_t) y << g.lnx) + x], o.wl[c]);
 			}
 			return;
 		}
@@ -270,13 +280,18 @@ struct F64 {
 		if(sm && lx >= 0 && ly >= 0 && lx + 1 < W && ly + 1 < W)
 		{
 			long long *p = reinterpret_cast<long long *>(sm) + ly * W + lx;
+			long long *q = p + W * W;
 			atomicAdd((unsigned long long *) &p[0], (unsigned long long) o.w[0]);
 			atomicAdd((unsigned long long *) &p[W], (unsigned long long) o.w[1]);
 			atomicAdd((unsigned long long *) &p[1], (unsigned long long) o.w[2]);
 			atomicAdd((unsigned long long *) &p[W + 1], (unsigned long long) o.w[3]);
+			atomicAdd((unsigned long long *) &q[0], (unsigned long long) o.wl[0]);
+			atomicAdd((unsigned long long *) &q[W], (unsigned long long) o.wl[1]);
+			atomicAdd((unsigned long long *) &q[1], (unsigned long long) o.wl[2]);
+			atomicAdd((unsigned long long *) &q[W + 1], (unsigned long long) o.wl[3]);
 		}
 		else
-			dep_global(a.rho, g, tx0 + o.rx, ty0 + o.ry, o.w[0], o.w[1], o.w[2], o.w[3]);
+			dep_global2(a.rho, a.rho_lo, g, tx0 + o.rx, ty0 + o.ry, o.w, o.wl);
 	}
 
 	static __device__ __forceinline__ void flush(const PushArgs &a, int s, unsigned char *sm,
@@ -285,9 +300,10 @@ struct F64 {
 		const long long *acc = reinterpret_cast<const long long *>(sm);
 		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
 		{
-			long long v = acc[i];
-			if(v != 0)
-				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)], v);
+			long long v = acc[i], vl = acc[W * W + i];
+			int64_t node = frame_node(a.g, W, H, tx0, ty0, i);
+			if(v != 0) red_global(&a.rho[node], v);
+			if(vl != 0) red_global(&a.rho_lo[node], vl);
 		}
 	}
 

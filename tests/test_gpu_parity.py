@@ -130,19 +130,30 @@ def test_multistep_two_species_bz(lib):
     assert abs(g.diag()["Q"]) < 1e-9
 
 
+def charge_scale(case):
+    """Mean |charge| per node of each species, summed: the size of the terms
+    whose sum is rho.  In a neutral plasma the net rho is a small residual of
+    these, and a sequential FP64 sum (the reference's, the oracle's) is
+    accurate only to ~1e-16 of this scale, not of the residual."""
+    ng = case["nx"] * case["ny"]
+    return sum(len(s["x"]) * abs(s["q"]) for s in case["species"]) / ng
+
+
 def test_two_species_full_size(lib):
     """512x512, 16 electrons and 16 ions (mass ratio 100) per cell, Bz = 0.5:
-    8,388,608 particles.  Two stages bit-exact from identical fields, then
-    three full steps with field energy within 1e-10."""
+    8,388,608 particles.  Two stages bit-exact from identical fields (rho
+    within 1e-12 of the summed-term scale), then three full steps with field
+    energy within 1e-10."""
     case = cases.two_species()
     g, o = prepared(case)
-    assert rel_max(g.rho(), o.rho()) <= RHO_TOL
+    scale = charge_scale(case)
+    assert np.max(np.abs(g.rho() - o.rho())) <= RHO_TOL * scale
     for it in range(2):
         _one_stage(g, o)
         for s in range(2):
             for a, b in zip(g.particles(s), o.particles(s)):
                 assert np.array_equal(a, b), (it, s)
-        assert rel_max(g.rho(), o.rho()) <= RHO_TOL
+        assert np.max(np.abs(g.rho() - o.rho())) <= RHO_TOL * scale
         o.stage_field_E()
     g.stage_field_E()
     for k in range(3):
