@@ -1,0 +1,95 @@
+"""The reference's own physics tests, test/constant-speed.c and
+test/cyclotron.c with conf/constant-speed.conf and conf/cyclotron.conf,
+restated through the C ABI on the GPU.  Their drivers, linked unchanged
+against the drop-in sim layer, need the reference tree, which the GPU host
+does not have.
+
+- constant speed (constant-speed.c:76-101): one electron, q = -1, m = 0.01,
+  u = (1.33333, 0.282828) on a 64x64 grid of 32x32, dt = 0.5, 4 plasma
+  chunks, 50000 cycles; its own field must not change its velocity by more
+  than 1e-10 (FP64 form; the mixed form's FP32 field leaves a self-force of
+  FP32 rounding size, bounded separately).
+- cyclotron (cyclotron.c:80-236): one electron, q = -1, m = 1, u = (0, 10)
+  in B = (0, 0, -1) on a 4x4 grid, dt = 0.05, eps0 = 8.85e-12, 5000
+  cycles.  The driver's strict check (distance to the analytic orbit point
+  below v dt^2, WEAK_CHECK 0) is not met by the reference's own algorithm:
+  Boris rotates by 2 atan(w dt / 2) instead of w dt, a phase lag of about
+  (w dt)^3 / 12 per step, 0.52 after 5000 steps against a limit of 0.025 (the
+  oracle, pinned to the reference, reproduces exactly that).  So this test
+  checks its weak form (distance to the orbit centre equals the radius
+  within v dt^2, cyclotron.c:170-190), the phase lag against the Boris
+  formula, and the FP64 trajectory bit-exact against the oracle.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from cpic_gb300 import _lib
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _constant_speed(prec, steps):
+    c = _lib.Context(64, 64, 32.0, 32.0, 0.5, 1.0, (0.0, 0.0, 0.0), precision=prec,
+                     plasma_chunks=4, cycles=steps)
+    u0 = (1.33333, 0.282828)
+    c.add_species(-1.0, 1.0e-2, [4.0], [16.0], [u0[0]], [u0[1]])
+    c.pre_step()
+    ref = np.array(u0, np.float32 if prec == _lib.MIXED else np.float64).astype(np.float64)
+    worst = 0.0
+    for chunk in range(steps // 500):
+        c.run(500)
+        x, y, ux, uy = c.particles(0)
+        worst = max(worst, abs(ux[0] - ref[0]), abs(uy[0] - ref[1]))
+    assert c.iter == steps
+    return worst
+
+
+def test_constant_speed_fp64(lib):
+    assert _constant_speed(_lib.FP64, 50000) <= 1e-10
+
+
+def test_constant_speed_mixed(lib):
+    # FP32 E: the self-force cancels only to FP32 rounding of the node values
+    assert _constant_speed(_lib.MIXED, 50000) <= 1e-4 * math.hypot(1.33333, 0.282828)
+
+
+def _cyclotron_run(make, steps):
+    """Positions after each of `steps` steps (step 1 = the half kick)."""
+    sim = make()
+    sim.add_species(-1.0, 1.0, [2.0], [16.0], [0.0], [10.0])
+    sim.pre_step()
+    out = np.empty((steps, 2))
+    for k in range(steps):
+        sim.step()
+        x, y, _, _ = sim.particles(0)
+        out[k] = (x[0], y[0])
+    return out
+
+
+@pytest.mark.parametrize("prec", [_lib.FP64, _lib.MIXED], ids=["fp64", "mixed"])
+def test_cyclotron(lib, orc, prec):
+    dt, steps, v = 0.05, 5000, 10.0
+    B = (0.0, 0.0, -1.0)
+    gpu = _cyclotron_run(lambda: _lib.Context(4, 4, 32.0, 32.0, dt, 8.85e-12, B, precision=prec,
+                                              plasma_chunks=4, cycles=steps), steps)
+    # orbit centre from the initial state, as cyclotron_postinit does:
+    # c = r0 + (u x B) * radius / |u x B|, radius = v / (|q| Bz / m) = -10
+    freq = -1.0
+    radius = v / freq
+    uxB = np.cross([0.0, v, 0.0], B)
+    center = np.array([2.0, 16.0]) + (uxB * radius / np.linalg.norm(uxB))[:2]
+    r = gpu - center
+    dist = np.hypot(r[:, 0], r[:, 1])
+    assert np.max(np.abs(dist - abs(radius))) <= v * dt * dt
+    # phase lag after the half kick: (steps - 1) Boris rotations of
+    # 2 atan(w dt / 2) against w dt
+    ang = np.unwrap(np.arctan2(r[:, 1], r[:, 0]))
+    lag = abs((ang[-1] - ang[0])) - (steps - 1) * 2 * math.atan(dt / 2)
+    assert abs(lag) <= 1e-6 * steps
+    if prec == _lib.FP64:
+        ref = _cyclotron_run(lambda: oracle.Oracle(4, 4, 32.0, 32.0, dt, 8.85e-12, B,
+                                                   plasma_chunks=4), steps)
+        assert np.array_equal(gpu, ref)
