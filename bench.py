@@ -253,8 +253,7 @@ def run_ours(args):
     if not args.no_e2e:
         e2e_steps = max(args.steps, args.e2e_steps)
         from cpic_gb300 import _lib as L
-        host = {k: st[k] for k in ("x", "y", "ux", "uy")}
-        outx = [np.empty(n) for _ in range(4)]
+        host, outx = pinned_state(st, n)
         barrier()
         t0 = time.perf_counter()
         ctx = make_ctx(grid, st, prec, dt)
@@ -271,6 +270,7 @@ def run_ours(args):
                       "seconds": el,
                       "h2d_bytes_per_step": 4 * 8 * n / e2e_steps,
                       "d2h_bytes_per_step": 4 * 8 * n / e2e_steps + 5 * 8,
+                      "host_memory": "pinned" if host["x"].base is not None else "pageable",
                       "path": "cpic_create/cpic_add_species/cpic_pre_step, per step cpic_run(1) + "
                               "cpic_field_energy read-back, cpic_get_particles"}
 
@@ -278,6 +278,24 @@ def run_ours(args):
     if rank == 0 and ws == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(grid, ppc, v0, vth, amp, dt, n, threads=1)
     return out
+
+
+def pinned_state(st, n):
+    """The initial state and the download buffers in page-locked host
+    memory (filled before the timed region)."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError
+        def buf():
+            return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        host = {}
+        for k in ("x", "y", "ux", "uy"):
+            host[k] = buf()
+            np.copyto(host[k], st[k])
+        return host, [buf() for _ in range(4)]
+    except Exception:
+        return {k: st[k] for k in ("x", "y", "ux", "uy")}, [np.empty(n) for _ in range(4)]
 
 
 def _oracle_sample(grid, ppc, v0, vth, amp, dt, frac, seed):
@@ -436,6 +454,151 @@ def study_accuracy(args):
     return res
 
 
+def ensemble_members(nruns, seed=2024):
+    """Seeded ensemble: grid side from {32, 64, 128, 256}, 8-128 particles
+    per cell, beam speed in [0.1, 0.4], perturbation amplitude in
+    [0.001, 0.05]; cold two-stream beams, dt 0.05, L = 2 pi."""
+    rng = np.random.default_rng(seed)
+    grid = rng.choice([32, 64, 128, 256], nruns)
+    ppc = rng.integers(8, 129, nruns)
+    v0 = rng.uniform(0.1, 0.4, nruns)
+    amp = rng.uniform(0.001, 0.05, nruns)
+    return [dict(grid=int(g), ppc=int(c), v0=float(v), amp=float(a), seed=i + 1)
+            for i, (g, c, v, a) in enumerate(zip(grid, ppc, v0, amp))]
+
+
+def _member_ctx(m, precision, tile):
+    from cpic_gb300 import _lib
+    L = 2 * math.pi
+    n = m["grid"] * m["grid"] * m["ppc"]
+    x, y, ux, uy = _lib.init_two_stream(m["seed"], 0, n, L, L, m["v0"], 0.0, m["amp"])
+    q = -L * L / n
+    c = _lib.Context(m["grid"], m["grid"], L, L, 0.05, 1.0, (0.0, 0.0, 0.0), precision=precision,
+                     track_ids=False, tile=tile)
+    c.add_species(q, -q, x, y, ux, uy)
+    c.pre_step()
+    return c, n
+
+
+def study_ensemble(args):
+    """Batched ensemble: every run of the ensemble stepped by one CUDA graph
+    (after autotuning the tile per (grid, particles per cell)), against the
+    same runs stepped one after another; per-run field-energy error of the
+    mixed form against the FP64 form over the first 300 steps."""
+    from cpic_gb300 import _lib, build
+    import torch
+    build.build()
+    L = 2 * math.pi
+    members = ensemble_members(args.ensemble_runs)
+    steps = args.ensemble_steps
+    t0 = time.perf_counter()
+    tiles = {}
+    for m in members:
+        key = (m["grid"], int(round(math.log2(m["ppc"]))))
+        if key not in tiles:
+            n = m["grid"] * m["grid"] * m["ppc"]
+            tiles[key] = _lib.autotune_tile(m["grid"], m["grid"], L, L, 0.05, n, m["v0"], 0.0)[0]
+        m["tile"] = tiles[key]
+    t_tune = time.perf_counter() - t0
+    res = {"study": "ensemble", "runs": len(members), "steps": steps, "precision": "mixed",
+           "particles_total": int(sum(m["grid"] ** 2 * m["ppc"] for m in members)),
+           "autotune_seconds": t_tune,
+           "autotuned_tiles": {"%dx%d ppc~2^%d" % (k[0], k[0], k[1]): v for k, v in sorted(tiles.items())}}
+    pstep = res["particles_total"] * steps
+    # one graph for all runs
+    runs = [_member_ctx(m, _lib.MIXED, m["tile"])[0] for m in members]
+    ens = _lib.Ensemble(runs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ms_graph, caps = ens.run(steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    res.update({"graph_wall_s": wall, "graph_ms_device": ms_graph, "graph_captures": caps,
+                "runs_per_s": len(members) / wall, "particle_steps_per_s": pstep / wall})
+    ens.close()
+    for c in runs:
+        c.close()
+    del runs
+    # the same runs one after another, no graph
+    t_seq = 0.0
+    for m in members:
+        c, n = _member_ctx(m, _lib.MIXED, m["tile"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c.run(steps)
+        torch.cuda.synchronize()
+        t_seq += time.perf_counter() - t0
+        c.close()
+    res.update({"sequential_wall_s": t_seq, "sequential_runs_per_s": len(members) / t_seq,
+                "graph_speedup": t_seq / wall})
+    # per-run error against the FP64 form
+    if not args.no_fp64:
+        lin = min(300, steps)
+        errs = []
+        for m in members:
+            cm, _ = _member_ctx(m, _lib.MIXED, m["tile"])
+            cf, _ = _member_ctx(m, _lib.FP64, 0)
+            worst = 0.0
+            for k in range(0, lin, 20):
+                cm.run(20)
+                cf.run(20)
+                a, b = cm.field_energy(), cf.field_energy()
+                worst = max(worst, abs(a - b) / b)
+            errs.append(worst)
+            cm.close()
+            cf.close()
+        errs = np.array(errs)
+        res.update({"we_rel_err_vs_fp64": {"steps": lin, "median": float(np.median(errs)),
+                                           "p90": float(np.quantile(errs, 0.9)),
+                                           "max": float(errs.max()),
+                                           "runs_below_1e-5": int(np.sum(errs <= 1e-5))}})
+    return res
+
+
+def study_adjoint(args):
+    """Adjoint of the field energy after 200 steps (128x128, 64 electrons
+    per cell, v0 0.2, amplitude 0.01, checkpoint every 20): cost against the
+    forward run, FP64 and FP32, and the gradients with respect to v0 and the
+    amplitude against FP64 central finite differences (eps 1e-6)."""
+    from cpic_gb300 import _lib, build
+    build.build()
+    L = 2 * math.pi
+    grid, ppc, steps, K = 128, 64, 200, 20
+    n = grid * grid * ppc
+    q = -L * L / n
+    xt, y, _, _ = _lib.init_two_stream(11, 0, n, L, L, 1.0, 0.0, 0.0)
+    sign = np.where(np.arange(n) < n // 2, 1.0, -1.0)
+    sx = np.sin(2 * math.pi * xt / L)
+    zeros = np.zeros(n)
+
+    def state(v0, amp):
+        return np.mod(xt + amp * sx, L), y, sign * v0, zeros
+
+    res = {"study": "adjoint", "grid": grid, "particles": n, "steps": steps, "checkpoint_every": K}
+    fd = {}
+    for name, prec in (("fp64", _lib.FP64), ("fp32", _lib.MIXED)):
+        adj = _lib.Adjoint(grid, grid, L, L, 0.05, 1.0, q, -q, n, steps, K, precision=prec)
+        adj.forward(*state(0.2, 0.01))
+        adj.backward()
+        loss = adj.forward(*state(0.2, 0.01))
+        g = adj.backward()
+        tf, tb = adj.times()
+        dv0 = float(np.sum(sign * g[2]))
+        damp = float(np.sum(sx * g[0]))
+        r = {"loss": loss, "dL_dv0": dv0, "dL_damp": damp, "ms_forward": tf, "ms_backward": tb,
+             "backward_over_forward": tb / tf}
+        if prec == _lib.FP64:
+            eps = 1e-6
+            fd["v0"] = (adj.forward(*state(0.2 + eps, 0.01)) - adj.forward(*state(0.2 - eps, 0.01))) / (2 * eps)
+            fd["amp"] = (adj.forward(*state(0.2, 0.01 + eps)) - adj.forward(*state(0.2, 0.01 - eps))) / (2 * eps)
+            res["fd_fp64"] = {"dL_dv0": fd["v0"], "dL_damp": fd["amp"]}
+        r["rel_err_vs_fd"] = {"v0": abs(dv0 - fd["v0"]) / abs(fd["v0"]),
+                              "amp": abs(damp - fd["amp"]) / abs(fd["amp"])}
+        res[name] = r
+        adj.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -446,8 +609,12 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--accuracy-steps", type=int, default=300,
                     help="steps of the mixed-vs-FP64 field-energy comparison (linear phase)")
-    ap.add_argument("--study", default="", choices=["", "accuracy"],
-                    help="accuracy: long mixed-vs-FP64 run (growth rate, energy drift), no timing")
+    ap.add_argument("--study", default="", choices=["", "accuracy", "ensemble", "adjoint"],
+                    help="accuracy: long mixed-vs-FP64 run (growth rate, energy drift), no timing; "
+                    "ensemble: batched independent runs in one CUDA graph; adjoint: gradient "
+                    "cost and finite-difference check")
+    ap.add_argument("--ensemble-runs", type=int, default=256)
+    ap.add_argument("--ensemble-steps", type=int, default=400)
     ap.add_argument("--study-steps", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-fp64", action="store_true")
@@ -467,6 +634,10 @@ def main():
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     if args.study == "accuracy":
         out = study_accuracy(args) if rank == 0 else None
+    elif args.study == "ensemble":
+        out = study_ensemble(args) if rank == 0 else None
+    elif args.study == "adjoint":
+        out = study_adjoint(args) if rank == 0 else None
     else:
         out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if rank == 0 and out is not None:

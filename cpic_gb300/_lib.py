@@ -39,6 +39,17 @@ class Params(ctypes.Structure):
     ]
 
 
+class AdjParams(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int64), ("ny", ctypes.c_int64),
+        ("Lx", ctypes.c_double), ("Ly", ctypes.c_double),
+        ("dt", ctypes.c_double), ("e0", ctypes.c_double),
+        ("q", ctypes.c_double), ("m", ctypes.c_double), ("Bz", ctypes.c_double),
+        ("nsteps", ctypes.c_int64), ("checkpoint_every", ctypes.c_int64),
+        ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
+    ]
+
+
 _LIB = None
 D = ctypes.POINTER(ctypes.c_double)
 
@@ -72,6 +83,19 @@ SIGNATURES = [
     ("cpic_tile_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
     ("cpic_poisson_noalloc", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                             ctypes.c_int64, ctypes.c_void_p]),
+    ("cpic_ensemble_create", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_void_p)]),
+    ("cpic_ensemble_destroy", None, [ctypes.c_void_p]),
+    ("cpic_ensemble_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, D,
+                                         ctypes.POINTER(ctypes.c_int32)]),
+    ("cpic_autotune_tile", ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, ctypes.c_double,
+                                          ctypes.c_double, ctypes.POINTER(ctypes.c_int32), D]),
+    ("cpic_adj_create", ctypes.c_int, [ctypes.POINTER(AdjParams), ctypes.c_int64,
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    ("cpic_adj_destroy", None, [ctypes.c_void_p]),
+    ("cpic_adj_forward", ctypes.c_int, [ctypes.c_void_p, D, D, D, D, D]),
+    ("cpic_adj_backward", ctypes.c_int, [ctypes.c_void_p, D, D, D, D]),
+    ("cpic_adj_times", ctypes.c_int, [ctypes.c_void_p, D, D]),
     ("cpic_uniform", None, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64, D]),
     ("cpic_normal", None, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64, D]),
     ("cpic_init_two_stream", None, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int64,
@@ -259,3 +283,99 @@ class Context:
         out = (ctypes.c_int32 * 4)()
         self._check(self.lib.cpic_tile_info(self.h, out), "cpic_tile_info")
         return dict(tile_x=out[0], tile_y=out[1], halo=out[2], slack_pct=out[3])
+
+
+class Adjoint:
+    """Differentiable run (cpic_adj_t): loss = final field energy, gradient
+    with respect to the initial particle state."""
+
+    def __init__(self, nx, ny, Lx, Ly, dt, e0, q, m, n, nsteps, checkpoint_every, Bz=0.0,
+                 precision=FP64):
+        self.lib = load()
+        p = AdjParams()
+        p.nx, p.ny, p.Lx, p.Ly, p.dt, p.e0 = nx, ny, Lx, Ly, dt, e0
+        p.q, p.m, p.Bz = q, m, Bz
+        p.nsteps, p.checkpoint_every, p.precision = nsteps, checkpoint_every, precision
+        h = ctypes.c_void_p()
+        r = self.lib.cpic_adj_create(ctypes.byref(p), n, ctypes.byref(h))
+        if r < 0:
+            raise CpicError(r, "cpic_adj_create")
+        self.h, self.n = h, n
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cpic_adj_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, x, y, ux, uy):
+        x, y, ux, uy = (_f64(a) for a in (x, y, ux, uy))
+        out = ctypes.c_double()
+        r = self.lib.cpic_adj_forward(self.h, _dp(x), _dp(y), _dp(ux), _dp(uy), ctypes.byref(out))
+        if r < 0:
+            raise CpicError(r, "cpic_adj_forward")
+        return out.value
+
+    def backward(self):
+        g = [np.empty(self.n, np.float64) for _ in range(4)]
+        r = self.lib.cpic_adj_backward(self.h, *[_dp(a) for a in g])
+        if r < 0:
+            raise CpicError(r, "cpic_adj_backward")
+        return g
+
+    def times(self):
+        f, b = ctypes.c_double(), ctypes.c_double()
+        self.lib.cpic_adj_times(self.h, ctypes.byref(f), ctypes.byref(b))
+        return f.value, b.value
+
+
+class Ensemble:
+    """Independent prepared runs (Context objects) stepped by one CUDA graph."""
+
+    def __init__(self, runs):
+        self.lib = load()
+        self.runs = list(runs)
+        arr = (ctypes.c_void_p * len(self.runs))(*[r.h.value for r in self.runs])
+        h = ctypes.c_void_p()
+        r = self.lib.cpic_ensemble_create(arr, len(self.runs), ctypes.byref(h))
+        if r < 0:
+            raise CpicError(r, "cpic_ensemble_create")
+        self.h = h
+
+    def run(self, nsteps):
+        ms = ctypes.c_double()
+        caps = ctypes.c_int32()
+        r = self.lib.cpic_ensemble_run(self.h, nsteps, ctypes.byref(ms), ctypes.byref(caps))
+        if r < 0:
+            raise CpicError(r, "cpic_ensemble_run")
+        return ms.value, caps.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cpic_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune_tile(nx, ny, Lx, Ly, dt, n, v0, vth, precision=MIXED, e0=1.0):
+    """(tile, ms per step) chosen by the library's autotuner."""
+    lib = load()
+    p = Params()
+    p.nx, p.ny, p.Lx, p.Ly, p.dt, p.e0 = nx, ny, Lx, Ly, dt, e0
+    p.plasma_chunks, p.precision = 1, precision
+    t = ctypes.c_int32()
+    ms = ctypes.c_double()
+    r = lib.cpic_autotune_tile(ctypes.byref(p), n, v0, vth, ctypes.byref(t), ctypes.byref(ms))
+    if r < 0:
+        raise CpicError(r, "cpic_autotune_tile")
+    return t.value, ms.value

@@ -26,6 +26,7 @@ UNITS = [
     ("cpic_fp64.cu", ["--fmad=false"]),
     ("cpic_mixed.cu", ["--fmad=true"]),
     ("cpic_noalloc.cu", ["--fmad=false"]),
+    ("cpic_adjoint.cu", ["--fmad=true"]),
 ]
 C_UNITS = ["cpic_init.c", "cpic_conf.c"]
 

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 
 #include "../../include/cpic_gpu.h"
 #include "cpic_common.cuh"
@@ -924,14 +925,21 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	SpeciesHost &S = c->sp[s];
 	memset((void *) &S, 0, sizeof(S));
 	S.q = q; S.m = m; S.n = n;
+	// comm_plasma's global exchange never wraps X (comm_plasma.c:826-870);
+	// checked on all host threads (hundreds of millions of particles)
+	int bad = 0;
+	double vmax = 0.0;
+	const double Lx = c->p.Lx;
+	#pragma omp parallel for schedule(static) reduction(max: vmax) reduction(|: bad)
 	for(int64_t i = 0; i < n; i++)
 	{
-		// comm_plasma's global exchange never wraps X (comm_plasma.c:826-870)
-		if(!(x[i] >= 0.0 && x[i] <= c->p.Lx) || !std::isfinite(y[i])
+		if(!(x[i] >= 0.0 && x[i] <= Lx) || !std::isfinite(y[i])
 				|| !std::isfinite(ux[i]) || !std::isfinite(uy[i]))
-			return CPIC_EINVAL;
-		S.vmax = std::max(S.vmax, std::max(fabs(ux[i]), fabs(uy[i])));
+			bad |= 1;
+		vmax = std::max(vmax, std::max(fabs(ux[i]), fabs(uy[i])));
 	}
+	if(bad) return CPIC_EINVAL;
+	S.vmax = vmax;
 	int nt = c->ntiles;
 	CK(cudaMalloc(&S.tiles.base, nt * sizeof(int64_t)));
 	CK(cudaMalloc(&S.tiles.cap, nt * sizeof(int32_t)));
@@ -967,7 +975,7 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	if(r) return r;
 	// halo: 1.2x the largest initial displacement per step, plus one
 	// (faster particles deposit through global memory: correct, slower)
-	double vmax = 0.0;
+	vmax = 0.0;
 	for(int k = 0; k < c->nspecies; k++) vmax = std::max(vmax, c->sp[k].vmax);
 	if(c->p.halo <= 0)
 	{
@@ -1344,6 +1352,263 @@ CPIC_API int cpic_tile_info(const cpic_ctx_t *c, int32_t *out)
 	out[1] = c->g.ty;
 	out[2] = c->g.halo;
 	out[3] = 25;
+	return CPIC_OK;
+}
+
+} // extern "C"
+
+// ------------------------------------------------------------------------
+// Ensembles: many independent runs stepped by one CUDA graph.
+//
+// Every step of a run is a fixed sequence of asynchronous launches whose
+// arguments depend only on the iteration being 0 or not and on the parity
+// of the double-buffered spill list, so two steps of every run (iteration
+// >= 1) are captured once -- each run on its own stream, forked from and
+// joined into one origin stream, i.e. independent branches of one graph --
+// and the executable graph is relaunched.  The host checks the runs'
+// status words every 16 steps; a run whose tile layout had to be rebuilt
+// (new store pointers) triggers one re-capture.
+
+struct cpic_ensemble {
+	std::vector<cpic_ctx *> runs;
+	cudaStream_t origin = nullptr;
+	cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+	std::vector<cudaEvent_t> join;
+	cudaGraphExec_t exec = nullptr;
+	int captures = 0;
+};
+
+static void ens_drop_graph(cpic_ensemble *e)
+{
+	if(e->exec) cudaGraphExecDestroy(e->exec);
+	e->exec = nullptr;
+}
+
+static int ens_capture(cpic_ensemble *e)
+{
+	ens_drop_graph(e);
+	cudaGraph_t graph = nullptr;
+	CK(cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeRelaxed));
+	int r = CPIC_OK;
+	if(cudaEventRecord(e->fork, e->origin) != cudaSuccess) r = CPIC_ECUDA;
+	for(size_t i = 0; i < e->runs.size() && r == CPIC_OK; i++)
+	{
+		cpic_ctx *c = e->runs[i];
+		if(cudaStreamWaitEvent(c->stream, e->fork, 0) != cudaSuccess) { r = CPIC_ECUDA; break; }
+		for(int k = 0; k < 2 && r == CPIC_OK; k++)
+		{
+			r = field_stage_async(c);
+			if(r == CPIC_OK) r = plasma_stage_async(c, false);
+		}
+		if(r == CPIC_OK && (cudaEventRecord(e->join[i], c->stream) != cudaSuccess
+				|| cudaStreamWaitEvent(e->origin, e->join[i], 0) != cudaSuccess))
+			r = CPIC_ECUDA;
+	}
+	cudaError_t ce = cudaStreamEndCapture(e->origin, &graph);
+	if(r) { if(graph) cudaGraphDestroy(graph); return r; }
+	if(ce != cudaSuccess) return CPIC_ECUDA;
+	ce = cudaGraphInstantiate(&e->exec, graph, 0);
+	cudaGraphDestroy(graph);
+	if(ce != cudaSuccess) { e->exec = nullptr; return CPIC_ECUDA; }
+	e->captures++;
+	return CPIC_OK;
+}
+
+// Status of every run after the origin stream drained; rebuilds the tile
+// layout of runs that spilled (the graph must then be captured again).
+static int ens_check(cpic_ensemble *e, bool *rebuilt)
+{
+	CK(cudaStreamSynchronize(e->origin));
+	*rebuilt = false;
+	for(cpic_ctx *c : e->runs)
+	{
+		int r = check_status(c);
+		if(r) return r;
+		for(int s = 0; s < c->nspecies; s++)
+		{
+			int32_t ns = 0;
+			CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
+					cudaMemcpyDeviceToHost));
+			if(ns > 0)
+			{
+				if((r = rebuild_species(c, s, false, nullptr, 0))) return r;
+				*rebuilt = true;
+			}
+		}
+	}
+	return CPIC_OK;
+}
+
+extern "C" {
+
+CPIC_API int cpic_ensemble_create(cpic_ctx_t *const *runs, int32_t nruns, cpic_ensemble_t **out)
+{
+	if(!runs || nruns <= 0 || !out) return CPIC_EINVAL;
+	*out = nullptr;
+	for(int32_t i = 0; i < nruns; i++)
+		if(!runs[i] || !runs[i]->prepared) return CPIC_ESTATE;
+	cpic_ensemble *e = new cpic_ensemble();
+	e->runs.assign(runs, runs + nruns);
+	e->join.resize(nruns, nullptr);
+	int r = CPIC_OK;
+	if(cudaStreamCreateWithFlags(&e->origin, cudaStreamNonBlocking) != cudaSuccess
+			|| cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess
+			|| cudaEventCreate(&e->t0) != cudaSuccess || cudaEventCreate(&e->t1) != cudaSuccess)
+		r = CPIC_ECUDA;
+	for(int32_t i = 0; i < nruns && r == CPIC_OK; i++)
+		if(cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming) != cudaSuccess)
+			r = CPIC_ECUDA;
+	if(r) { cpic_ensemble_destroy(e); return r; }
+	*out = e;
+	return CPIC_OK;
+}
+
+CPIC_API void cpic_ensemble_destroy(cpic_ensemble_t *e)
+{
+	if(!e) return;
+	ens_drop_graph(e);
+	for(cudaEvent_t ev : e->join) if(ev) cudaEventDestroy(ev);
+	if(e->fork) cudaEventDestroy(e->fork);
+	if(e->t0) cudaEventDestroy(e->t0);
+	if(e->t1) cudaEventDestroy(e->t1);
+	if(e->origin) cudaStreamDestroy(e->origin);
+	delete e;
+}
+
+CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_graph,
+		int32_t *captures)
+{
+	if(!e || nsteps < 0) return CPIC_EINVAL;
+	int r;
+	for(cpic_ctx *c : e->runs)
+		if(c->p.cycles > 0 && c->iter + nsteps > c->p.cycles) return CPIC_EDONE;
+	int64_t done = 0;
+	// iteration 0 (the half kick has its own arguments): eagerly, all runs
+	// in flight on their own streams
+	bool first = false;
+	for(cpic_ctx *c : e->runs)
+		if(c->iter == 0) first = true;
+	if(first && nsteps > 0)
+	{
+		for(cpic_ctx *c : e->runs)
+		{
+			if(c->iter != 0) return CPIC_ESTATE;
+			if((r = field_stage_async(c)) || (r = plasma_stage_async(c, false))) return r;
+			c->iter++;
+		}
+		bool rebuilt;
+		for(cpic_ctx *c : e->runs) CK(cudaStreamSynchronize(c->stream));
+		if((r = ens_check(e, &rebuilt))) return r;
+		if(rebuilt) ens_drop_graph(e);
+		done = 1;
+	}
+	// the graph carries two steps; the spill parity of every run must be
+	// the one it was captured with
+	float tms = 0.0f;
+	int64_t pairs = (nsteps - done) / 2;
+	if(pairs > 0)
+	{
+		if(!e->exec && (r = ens_capture(e))) return r;
+		CK(cudaEventRecord(e->t0, e->origin));
+		float acc = 0.0f;
+		for(int64_t k = 0; k < pairs; k++)
+		{
+			CK(cudaGraphLaunch(e->exec, e->origin));
+			for(cpic_ctx *c : e->runs) c->iter += 2;
+			if((k & 7) == 7 || k + 1 == pairs)
+			{
+				CK(cudaEventRecord(e->t1, e->origin));
+				bool rebuilt;
+				if((r = ens_check(e, &rebuilt))) return r;
+				float part = 0.0f;
+				CK(cudaEventElapsedTime(&part, e->t0, e->t1));
+				acc += part;
+				if(rebuilt)
+				{
+					if(k + 1 < pairs) { if((r = ens_capture(e))) return r; }
+					else ens_drop_graph(e);
+				}
+				CK(cudaEventRecord(e->t0, e->origin));
+			}
+		}
+		tms = acc;
+		done += 2 * pairs;
+	}
+	// an odd last step, eagerly
+	if(done < nsteps)
+	{
+		CK(cudaStreamSynchronize(e->origin));
+		for(cpic_ctx *c : e->runs)
+		{
+			if((r = field_stage_async(c)) || (r = plasma_stage_async(c, false))) return r;
+			c->iter++;
+		}
+		for(cpic_ctx *c : e->runs) CK(cudaStreamSynchronize(c->stream));
+		bool rebuilt;
+		if((r = ens_check(e, &rebuilt))) return r;
+		if(rebuilt) ens_drop_graph(e);
+	}
+	if(ms_graph) *ms_graph = tms;
+	if(captures) *captures = e->captures;
+	return CPIC_OK;
+}
+
+// Tile size (= the re-bin's counting-sort bin width) for a grid and a
+// particle count: each candidate runs a seeded two-stream plasma of n
+// particles for 3 + 6 steps, the fastest by CUDA events wins.  Results are
+// kept per (grid, log2 particles per cell, precision) for the process.
+CPIC_API int cpic_autotune_tile(const cpic_params_t *p, int64_t n, double v0, double vth,
+		int32_t *tile, double *ms_per_step)
+{
+	if(!p || n <= 0 || !tile) return CPIC_EINVAL;
+	struct Key { int64_t nx, ny; int lppc, prec; double ms; int32_t T; };
+	static std::vector<Key> cache;
+	static std::mutex mu;
+	double ppc = (double) n / ((double) p->nx * (double) p->ny);
+	int lppc = (int) lround(log2(ppc > 0 ? ppc : 1.0));
+	{
+		std::lock_guard<std::mutex> lk(mu);
+		for(const Key &k : cache)
+			if(k.nx == p->nx && k.ny == p->ny && k.lppc == lppc && k.prec == p->precision)
+			{
+				*tile = k.T;
+				if(ms_per_step) *ms_per_step = k.ms;
+				return CPIC_OK;
+			}
+	}
+	std::vector<double> x(n), y(n), ux(n), uy(n);
+	cpic_init_two_stream(1, 0, n, p->Lx, p->Ly, v0, vth, 0.01, x.data(), y.data(), ux.data(),
+			uy.data());
+	double q = -p->Lx * p->Ly / (double) n;
+	int32_t best = 0;
+	double best_ms = INFINITY;
+	for(int32_t T = 4; T <= 64; T *= 2)
+	{
+		if(p->nx % T || p->ny % T || (p->nx / T) * (p->ny / T) < 4) continue;
+		cpic_params_t q2 = *p;
+		q2.tile_x = q2.tile_y = T;
+		q2.cycles = 0;
+		cpic_ctx_t *c = nullptr;
+		int r = cpic_create(&q2, &c);
+		if(r) continue;
+		double ms = INFINITY;
+		if(cpic_add_species(c, q, -q, n, x.data(), y.data(), ux.data(), uy.data()) >= 0
+				&& cpic_pre_step(c) == CPIC_OK && cpic_step(c) == CPIC_OK
+				&& cpic_time_steps(c, 3, nullptr, nullptr, nullptr) == CPIC_OK)
+		{
+			double tot = 0.0;
+			if(cpic_time_steps(c, 6, &tot, nullptr, nullptr) == CPIC_OK) ms = tot / 6.0;
+		}
+		cpic_destroy(c);
+		if(ms < best_ms) { best_ms = ms; best = T; }
+	}
+	if(!best) return CPIC_EINVAL;
+	{
+		std::lock_guard<std::mutex> lk(mu);
+		cache.push_back(Key{p->nx, p->ny, lppc, p->precision, best_ms, best});
+	}
+	*tile = best;
+	if(ms_per_step) *ms_per_step = best_ms;
 	return CPIC_OK;
 }
 

@@ -201,6 +201,42 @@ __global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<T>::t *
 	}
 }
 
+// Real-valued input (ny x nx of T) -> spec, otherwise as k_rows_fwd.  Used
+// by the adjoint, whose source term (rho-bar) is not a charge sum.
+template <typename T>
+__global__ void k_rows_fwd_real(int nx, int log2nx, const T *in, typename Cx<T>::t *spec,
+		const typename Cx<T>::t *tw)
+{
+	typedef typename Cx<T>::t C;
+	extern __shared__ unsigned char smem_raw[];
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + nx;
+	int r0 = 2 * blockIdx.x;
+	int nh = nx / 2 + 1;
+	for(int i = threadIdx.x; i < nx; i += blockDim.x)
+	{
+		C z;
+		z.x = in[(int64_t) r0 * nx + i];
+		z.y = in[(int64_t) (r0 + 1) * nx + i];
+		a[i] = z;
+	}
+	__syncthreads();
+	C *Z = fft_smem<C>(a, b, nx, log2nx, 1, -1, tw);
+	for(int k = threadIdx.x; k < nh; k += blockDim.x)
+	{
+		C p = Z[k];
+		C q = Z[(nx - k) & (nx - 1)];
+		q.y = -q.y;
+		C A, B;
+		A.x = (p.x + q.x) * (T) 0.5;
+		A.y = (p.y + q.y) * (T) 0.5;
+		B.x = (p.y - q.y) * (T) 0.5;
+		B.y = -(p.x - q.x) * (T) 0.5;
+		spec[(int64_t) r0 * nh + k] = A;
+		spec[(int64_t) (r0 + 1) * nh + k] = B;
+	}
+}
+
 template <typename T>
 static void poisson_launch(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		typename Cx<T>::t *spec, const typename Cx<T>::t *twx, const typename Cx<T>::t *twy,
@@ -224,6 +260,29 @@ static void poisson_launch(const Grid &g, const long long *rho, double qinv, con
 	int cthreads = 512;
 	k_cols<T><<<(nh + cb - 1) / cb, cthreads, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy);
 	k_rows_inv<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, phi);
+}
+
+// out = IFFT(G FFT(in)) / (nx ny) for a real ny x nx input: the same linear
+// operator as poisson_launch (symmetric, so it is also its own adjoint).
+template <typename T>
+static void poisson_launch_real(const Grid &g, const T *in, typename Cx<T>::t *spec,
+		const typename Cx<T>::t *twx, const typename Cx<T>::t *twy, const double *cosx,
+		const double *cosy, T *out, cudaStream_t s)
+{
+	typedef typename Cx<T>::t C;
+	int log2nx = 0, log2ny = 0;
+	while((1 << log2nx) < g.nx) log2nx++;
+	while((1 << log2ny) < g.ny) log2ny++;
+	int rthreads = g.nx / 2 < 512 ? (g.nx / 2 < 32 ? 32 : g.nx / 2) : 512;
+	size_t rsm = 2 * (size_t) g.nx * sizeof(C);
+	k_rows_fwd_real<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, in, spec, twx);
+	int nh = g.nx / 2 + 1;
+	int cb = (int) ((128 * 1024) / (2 * (size_t) g.ny * sizeof(C)));
+	if(cb < 1) cb = 1;
+	if(cb > nh) cb = nh;
+	size_t csm = 2 * (size_t) cb * g.ny * sizeof(C);
+	k_cols<T><<<(nh + cb - 1) / cb, 512, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy);
+	k_rows_inv<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, out);
 }
 
 } // namespace cpic

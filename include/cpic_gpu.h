@@ -195,6 +195,76 @@ CPIC_API int cpic_tile_info(const cpic_ctx_t *ctx, int32_t *out);
 CPIC_API int cpic_poisson_noalloc(const double *rho, double *phi, int64_t nx, int64_t ny,
 		void *stream);
 
+/* --- ensembles of independent runs ------------------------------------ */
+
+/* No counterpart in the reference (one run per MPI job there).  Groups
+ * prepared contexts (after cpic_pre_step, on the current device; not owned
+ * by the ensemble) of any grid sizes and particle counts. */
+typedef struct cpic_ensemble cpic_ensemble_t;
+
+CPIC_API int cpic_ensemble_create(cpic_ctx_t *const *runs, int32_t nruns,
+		cpic_ensemble_t **out);
+CPIC_API void cpic_ensemble_destroy(cpic_ensemble_t *e);
+
+/* nsteps steps of every run.  Iteration 0 runs eagerly; then one CUDA graph
+ * holding two steps of every run (each run an independent branch) is
+ * captured once and relaunched, the runs' status checked every 16 steps
+ * (a run whose tile layout is rebuilt causes one re-capture).  ms_graph:
+ * CUDA-event time of the graph launches; captures: graphs captured so far
+ * (either may be NULL). */
+CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_graph,
+		int32_t *captures);
+
+/* Autotuner: the tile size (cells per side; it is also the counting-sort
+ * bin width of the re-bin) for grid p->nx x p->ny, precision p->precision
+ * and n particles, chosen by timing a seeded two-stream plasma (beam speed
+ * v0, spread vth) with each candidate.  Cached per (grid, log2 particles
+ * per cell, precision) for the process. */
+CPIC_API int cpic_autotune_tile(const cpic_params_t *p, int64_t n, double v0, double vth,
+		int32_t *tile, double *ms_per_step);
+
+/* --- adjoint: gradient of the final field energy ---------------------- */
+
+/* No counterpart in the reference.  A differentiable run of the step for one
+ * species: nsteps calls of the step (iteration 0, the backward half kick,
+ * included) from an initial state (x, y, ux, uy), then the loss
+ * L = 1/2 e0 dx dy sum over nodes of |E|^2, with E solved from the charge of
+ * the final positions.  The backward sweep gives dL/dx, dL/dy, dL/dux,
+ * dL/duy of every initial particle by hand-written adjoint kernels: the
+ * gather's adjoint is a deposit, the deposit's a gather of the weight
+ * gradients, the Boris kick's the transposed rotation, the Poisson solve is
+ * its own adjoint.  States are kept every checkpoint_every steps and
+ * recomputed in between.  Precision CPIC_FP64, or CPIC_MIXED for FP32 state,
+ * fields and adjoint (charge sums stay 64-bit fixed point in both). */
+typedef struct cpic_adj_params {
+	int64_t nx, ny;           /* powers of two */
+	double Lx, Ly, dt, e0;
+	double q, m;              /* the species' macro charge and mass */
+	double Bz;                /* magnetic field along z */
+	int64_t nsteps;           /* >= 1 */
+	int64_t checkpoint_every; /* K >= 1 */
+	int32_t precision;
+	int32_t reserved[7];
+} cpic_adj_params_t;
+
+typedef struct cpic_adj cpic_adj_t;
+
+CPIC_API int cpic_adj_create(const cpic_adj_params_t *p, int64_t n, cpic_adj_t **out);
+CPIC_API void cpic_adj_destroy(cpic_adj_t *a);
+
+/* Uploads the initial state (host FP64, positions in [0,Lx) x [0,Ly)),
+ * runs the nsteps forward, keeping the checkpoints, and returns L. */
+CPIC_API int cpic_adj_forward(cpic_adj_t *a, const double *x, const double *y,
+		const double *ux, const double *uy, double *loss);
+
+/* After cpic_adj_forward: the gradient of L with respect to the initial
+ * state (host FP64 arrays of n; any may be NULL). */
+CPIC_API int cpic_adj_backward(cpic_adj_t *a, double *gx, double *gy, double *gux,
+		double *guy);
+
+/* CUDA-event durations of the last forward and backward sweeps, ms. */
+CPIC_API int cpic_adj_times(const cpic_adj_t *a, double *ms_forward, double *ms_backward);
+
 /* --- seeded initial states (host only; no GPU needed) ----------------- */
 
 /* The i-th uniform / normal draw of (seed, stream), i < n. */
