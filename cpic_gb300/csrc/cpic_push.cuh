@@ -638,6 +638,10 @@ k_push(const PushArgs a)
 	__shared__ __align__(8) uint64_t bars[2];
 	__shared__ __align__(8) uint64_t ebars[2];
 	__shared__ int s_cursor;
+	// base and capacity of the 3 x 3 tiles around this one: nearly every
+	// mover lands there, so its slot needs no dependent global loads
+	__shared__ int64_t s_nbase[9];
+	__shared__ int32_t s_ncap[9];
 	const Grid &g = a.g;
 	const int s = blockIdx.y;
 	const int t = blockIdx.x;
@@ -659,6 +663,17 @@ k_push(const PushArgs a)
 	const int n = T.cnt[t];
 	const int64_t base = T.base[t];
 	const int nchunks = (n + kChunk - 1) / kChunk;
+	const int ltx_n = g.lnx - g.ltx;                 // log2 tiles per row
+	const int ttx = t & (g.ntx - 1), tty = t >> ltx_n;
+	// neighbours are distinct tiles only with at least 3 tiles per side
+	const bool nb_ok = g.ntx >= 3 && g.nty >= 3;
+	if(threadIdx.x < 9 && nb_ok)
+	{
+		int dx = (int) threadIdx.x % 3 - 1, dy = (int) threadIdx.x / 3 - 1;
+		int nt = (((tty + dy) & (g.nty - 1)) << ltx_n) + ((ttx + dx) & (g.ntx - 1));
+		s_nbase[threadIdx.x] = T.base[nt];
+		s_ncap[threadIdx.x] = T.cap[nt];
+	}
 	if(threadIdx.x == 0)
 	{
 		s_cursor = 0;
@@ -751,8 +766,23 @@ k_push(const PushArgs a)
 			const int slot = warp_reserve_finish(rv[k], move);
 			if(move)
 			{
-				if(slot < T.cap[dest[k]])
-					F::store(a, s, T.base[dest[k]] + slot, rec[k]);
+				const int d = dest[k];
+				const int ddx = ((d & (g.ntx - 1)) - ttx + 1) & (g.ntx - 1);
+				const int ddy = ((d >> ltx_n) - tty + 1) & (g.nty - 1);
+				int64_t db;
+				int32_t dc;
+				if(nb_ok && ddx < 3 && ddy < 3)
+				{
+					db = s_nbase[ddy * 3 + ddx];
+					dc = s_ncap[ddy * 3 + ddx];
+				}
+				else
+				{
+					db = T.base[d];
+					dc = T.cap[d];
+				}
+				if(slot < dc)
+					F::store(a, s, db + slot, rec[k]);
 				else
 				{
 					double x, y, ux, uy;
