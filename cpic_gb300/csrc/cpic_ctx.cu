@@ -51,6 +51,7 @@ struct cpic_ctx {
 	int precision;
 	int64_t iter;
 	bool prepared;
+	int slack_pct = 25;       // tile capacity slack, grows after overflows
 	double qscale, qinv;
 	double qlo_mul, qinv_lo;  // FP64 form: remainder-word scales
 	cudaStream_t stream;
@@ -555,13 +556,15 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	CK(cudaMemcpyAsync(hc.data(), newcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
 
-	// capacities: 25% slack plus 64 slots, rounded to 32
+	// capacities: slack_pct % slack (25 % at first, doubled after every
+	// rebuild forced by an overflow, up to 200 %) plus 64 slots, rounded
+	// to 32
 	std::vector<int64_t> hb(nt);
 	std::vector<int32_t> hcap(nt);
 	int64_t total = 0, n = 0;
 	for(int t = 0; t < nt; t++)
 	{
-		int64_t cap = hc[t] + hc[t] / 4 + 64;
+		int64_t cap = hc[t] + hc[t] * c->slack_pct / 100 + 64;
 		cap = (cap + 31) & ~(int64_t) 31;
 		if(cap > INT32_MAX) return CPIC_ECAPACITY;
 		hb[t] = total;
@@ -636,6 +639,8 @@ static int rebuild_if_spilled(cpic_ctx *c)
 				cudaMemcpyDeviceToHost));
 		if(ns > 0)
 		{
+			// a tile overflowed: more headroom from now on
+			c->slack_pct = std::min(200, 2 * c->slack_pct);
 			int r = rebuild_species(c, s, false, nullptr, 0);
 			if(r) return r;
 		}
@@ -949,7 +954,8 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	CK(cudaMemset(S.tiles.cnt, 0, nt * sizeof(int32_t)));
 	CK(cudaMemset(S.tiles.app, 0, nt * sizeof(int32_t)));
 	CK(cudaMemset(S.tiles.stay, 0, nt * sizeof(int32_t)));
-	int32_t scap = (int32_t) std::max<int64_t>(65536, n / 32);
+	// room for an eighth of the species to overflow between two host checks
+	int32_t scap = (int32_t) std::max<int64_t>(65536, n / 8);
 	int r;
 	if((r = alloc_spill(S.spill[0], scap))) return r;
 	if((r = alloc_spill(S.spill[1], scap))) return r;
@@ -1043,7 +1049,7 @@ CPIC_API int cpic_run(cpic_ctx_t *c, int64_t nsteps)
 		if(r) return r;
 		if((r = plasma_stage_async(c, false))) return r;
 		c->iter++;
-		if((k & 15) == 15 || k + 1 == nsteps)
+		if((k & 7) == 7 || k + 1 == nsteps)
 		{
 			if((r = check_status(c))) return r;
 			if((r = rebuild_if_spilled(c))) return r;
@@ -1351,7 +1357,7 @@ CPIC_API int cpic_tile_info(const cpic_ctx_t *c, int32_t *out)
 	out[0] = c->g.tx;
 	out[1] = c->g.ty;
 	out[2] = c->g.halo;
-	out[3] = 25;
+	out[3] = c->slack_pct;
 	return CPIC_OK;
 }
 
@@ -1366,15 +1372,39 @@ CPIC_API int cpic_tile_info(const cpic_ctx_t *c, int32_t *out)
 // >= 1) are captured once -- each run on its own stream, forked from and
 // joined into one origin stream, i.e. independent branches of one graph --
 // and the executable graph is relaunched.  The host checks the runs'
-// status words every 16 steps; a run whose tile layout had to be rebuilt
+// status words every 4 steps; a run whose tile layout had to be rebuilt
 // (new store pointers) triggers one re-capture.
+
+// Per run: its status word and the spill list each species wrote last.
+struct EnsProbe {
+	const uint32_t *status;
+	const int32_t *spill[kMaxSpecies];
+	int nspecies;
+};
+
+// out[2 i] = status bits of run i, out[2 i + 1] = its largest spill count.
+__global__ void k_ens_status(int nruns, const EnsProbe *pr, int32_t *out)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < nruns; i += gridDim.x * blockDim.x)
+	{
+		int32_t m = 0;
+		for(int s = 0; s < pr[i].nspecies; s++) m = max(m, *pr[i].spill[s]);
+		out[2 * i] = (int32_t) *pr[i].status;
+		out[2 * i + 1] = m;
+	}
+}
 
 struct cpic_ensemble {
 	std::vector<cpic_ctx *> runs;
+	EnsProbe *probe_d = nullptr;
+	int32_t *probe_out_d = nullptr;
+	std::vector<EnsProbe> probe_h;
+	std::vector<int32_t> probe_out_h;
 	cudaStream_t origin = nullptr;
 	cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
 	std::vector<cudaEvent_t> join;
 	cudaGraphExec_t exec = nullptr;
+	bool stale = false;       // a run's layout changed since the capture
 	int captures = 0;
 };
 
@@ -1386,7 +1416,6 @@ static void ens_drop_graph(cpic_ensemble *e)
 
 static int ens_capture(cpic_ensemble *e)
 {
-	ens_drop_graph(e);
 	cudaGraph_t graph = nullptr;
 	CK(cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeRelaxed));
 	int r = CPIC_OK;
@@ -1407,34 +1436,70 @@ static int ens_capture(cpic_ensemble *e)
 	cudaError_t ce = cudaStreamEndCapture(e->origin, &graph);
 	if(r) { if(graph) cudaGraphDestroy(graph); return r; }
 	if(ce != cudaSuccess) return CPIC_ECUDA;
+	e->captures++;
+	e->stale = false;
+	if(e->exec)
+	{
+		// same launches with new pointers (a rebuilt layout): update the
+		// executable graph in place when the topology allows it
+		cudaGraphExecUpdateResultInfo info;
+		if(cudaGraphExecUpdate(e->exec, graph, &info) == cudaSuccess)
+		{
+			cudaGraphDestroy(graph);
+			return CPIC_OK;
+		}
+		cudaGetLastError();
+		ens_drop_graph(e);
+	}
 	ce = cudaGraphInstantiate(&e->exec, graph, 0);
 	cudaGraphDestroy(graph);
 	if(ce != cudaSuccess) { e->exec = nullptr; return CPIC_ECUDA; }
-	e->captures++;
 	return CPIC_OK;
 }
 
-// Status of every run after the origin stream drained; rebuilds the tile
-// layout of runs that spilled (the graph must then be captured again).
+static int status_code(uint32_t st)
+{
+	if(st & ST_SPILL_FULL) return CPIC_ECAPACITY;
+	if(st & ST_UMAX) return CPIC_EUMAX;
+	if(st & ST_NAN) return CPIC_ENAN;
+	if(st & ST_RANGE) return CPIC_EINVAL;
+	if(st & ST_TIMEOUT) return CPIC_ETIMEOUT;
+	return CPIC_OK;
+}
+
+// Status of every run, gathered on the device into one small read-back
+// after the origin stream's work; rebuilds the tile layout of runs that
+// spilled (the graph must then be captured again).
 static int ens_check(cpic_ensemble *e, bool *rebuilt)
 {
-	CK(cudaStreamSynchronize(e->origin));
+	int nr = (int) e->runs.size();
 	*rebuilt = false;
-	for(cpic_ctx *c : e->runs)
+	for(int i = 0; i < nr; i++)
 	{
-		int r = check_status(c);
+		cpic_ctx *c = e->runs[i];
+		EnsProbe &p = e->probe_h[i];
+		p.status = c->status;
+		p.nspecies = c->nspecies;
+		for(int s = 0; s < c->nspecies; s++) p.spill[s] = c->sp[s].spill[c->spill_cur].count;
+	}
+	CK(cudaMemcpyAsync(e->probe_d, e->probe_h.data(), nr * sizeof(EnsProbe),
+			cudaMemcpyHostToDevice, e->origin));
+	k_ens_status<<<(nr + 255) / 256, 256, 0, e->origin>>>(nr, e->probe_d, e->probe_out_d);
+	CK(cudaMemcpyAsync(e->probe_out_h.data(), e->probe_out_d, 2 * nr * sizeof(int32_t),
+			cudaMemcpyDeviceToHost, e->origin));
+	CK(cudaStreamSynchronize(e->origin));
+	for(int i = 0; i < nr; i++)
+	{
+		int r = status_code((uint32_t) e->probe_out_h[2 * i]);
 		if(r) return r;
-		for(int s = 0; s < c->nspecies; s++)
-		{
-			int32_t ns = 0;
-			CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
-					cudaMemcpyDeviceToHost));
-			if(ns > 0)
-			{
-				if((r = rebuild_species(c, s, false, nullptr, 0))) return r;
-				*rebuilt = true;
-			}
-		}
+	}
+	for(int i = 0; i < nr; i++)
+	{
+		if(e->probe_out_h[2 * i + 1] <= 0) continue;
+		cpic_ctx *c = e->runs[i];
+		int r = rebuild_if_spilled(c);
+		if(r) return r;
+		*rebuilt = true;
 	}
 	return CPIC_OK;
 }
@@ -1458,6 +1523,11 @@ CPIC_API int cpic_ensemble_create(cpic_ctx_t *const *runs, int32_t nruns, cpic_e
 	for(int32_t i = 0; i < nruns && r == CPIC_OK; i++)
 		if(cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming) != cudaSuccess)
 			r = CPIC_ECUDA;
+	e->probe_h.resize(nruns);
+	e->probe_out_h.resize(2 * (size_t) nruns);
+	if(r == CPIC_OK && (cudaMalloc(&e->probe_d, nruns * sizeof(EnsProbe)) != cudaSuccess
+			|| cudaMalloc(&e->probe_out_d, 2 * nruns * sizeof(int32_t)) != cudaSuccess))
+		r = CPIC_ENOMEM;
 	if(r) { cpic_ensemble_destroy(e); return r; }
 	*out = e;
 	return CPIC_OK;
@@ -1472,6 +1542,8 @@ CPIC_API void cpic_ensemble_destroy(cpic_ensemble_t *e)
 	if(e->t0) cudaEventDestroy(e->t0);
 	if(e->t1) cudaEventDestroy(e->t1);
 	if(e->origin) cudaStreamDestroy(e->origin);
+	if(e->probe_d) cudaFree(e->probe_d);
+	if(e->probe_out_d) cudaFree(e->probe_out_d);
 	delete e;
 }
 
@@ -1499,7 +1571,7 @@ CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_gr
 		bool rebuilt;
 		for(cpic_ctx *c : e->runs) CK(cudaStreamSynchronize(c->stream));
 		if((r = ens_check(e, &rebuilt))) return r;
-		if(rebuilt) ens_drop_graph(e);
+		if(rebuilt) e->stale = true;
 		done = 1;
 	}
 	// the graph carries two steps; the spill parity of every run must be
@@ -1508,14 +1580,14 @@ CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_gr
 	int64_t pairs = (nsteps - done) / 2;
 	if(pairs > 0)
 	{
-		if(!e->exec && (r = ens_capture(e))) return r;
+		if((!e->exec || e->stale) && (r = ens_capture(e))) return r;
 		CK(cudaEventRecord(e->t0, e->origin));
 		float acc = 0.0f;
 		for(int64_t k = 0; k < pairs; k++)
 		{
 			CK(cudaGraphLaunch(e->exec, e->origin));
 			for(cpic_ctx *c : e->runs) c->iter += 2;
-			if((k & 7) == 7 || k + 1 == pairs)
+			if((k & 1) == 1 || k + 1 == pairs)
 			{
 				CK(cudaEventRecord(e->t1, e->origin));
 				bool rebuilt;
@@ -1526,7 +1598,7 @@ CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_gr
 				if(rebuilt)
 				{
 					if(k + 1 < pairs) { if((r = ens_capture(e))) return r; }
-					else ens_drop_graph(e);
+					else e->stale = true;
 				}
 				CK(cudaEventRecord(e->t0, e->origin));
 			}
@@ -1546,7 +1618,7 @@ CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_gr
 		for(cpic_ctx *c : e->runs) CK(cudaStreamSynchronize(c->stream));
 		bool rebuilt;
 		if((r = ens_check(e, &rebuilt))) return r;
-		if(rebuilt) ens_drop_graph(e);
+		if(rebuilt) e->stale = true;
 	}
 	if(ms_graph) *ms_graph = tms;
 	if(captures) *captures = e->captures;

@@ -752,19 +752,18 @@ k_push(const PushArgs a)
 		if(lane == 0 && nst)
 			wb = atomicAdd(&s_cursor, nst);
 		wb = __shfl_sync(0xffffffffu, wb, 0);
+		// one store per particle: its own tile's compacted prefix, or its
+		// slot in the destination tile, or the spill list
 		#pragma unroll
 		for(int k = 0; k < kPPT; k++)
 		{
-			if(bs[k] & (1u << lane))
-				F::store(a, s, base + wb + __popc(bs[k] & lanemask_lt()), rec[k]);
-			wb += __popc(bs[k]);
-		}
-		#pragma unroll
-		for(int k = 0; k < kPPT; k++)
-		{
+			const bool stay = (bs[k] >> lane) & 1u;
 			const bool move = dest[k] >= 0 && dest[k] != t;
 			const int slot = warp_reserve_finish(rv[k], move);
-			if(move)
+			int64_t at = -1;
+			if(stay)
+				at = base + wb + __popc(bs[k] & lanemask_lt());
+			else if(move)
 			{
 				const int d = dest[k];
 				const int ddx = ((d & (g.ntx - 1)) - ttx + 1) & (g.ntx - 1);
@@ -782,7 +781,7 @@ k_push(const PushArgs a)
 					dc = T.cap[d];
 				}
 				if(slot < dc)
-					F::store(a, s, db + slot, rec[k]);
+					at = db + slot;
 				else
 				{
 					double x, y, ux, uy;
@@ -790,6 +789,9 @@ k_push(const PushArgs a)
 					spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id, a.status);
 				}
 			}
+			if(at >= 0)
+				F::store(a, s, at, rec[k]);
+			wb += __popc(bs[k]);
 		}
 	}
 	__syncthreads();

@@ -67,7 +67,7 @@ struct gpu_sim
 	int64_t **pid;          /* per species: reference particle index by GPU id */
 	double *buf;            /* 4 * max(n) doubles: x y ux uy */
 	double *ebuf;           /* 2 * sum(n) doubles: E at the particles */
-	double *fbuf;           /* 2 * nx * ny doubles */
+	double *fbuf;           /* 2 * nx * (ny + 1) doubles */
 };
 
 #define GPU(sim) ((struct gpu_sim *) (sim)->solver)
@@ -315,9 +315,11 @@ sync_fields(sim_t *sim)
 	fill_view(f->rho, g->fbuf, nx, ny, 0);
 	if((rc = cpic_get_phi(g->ctx, g->fbuf))) { gpu_err("cpic_get_phi", rc); return -1; }
 	fill_view(f->phi, g->fbuf, nx, ny, 0);
-	if((rc = cpic_get_E(g->ctx, g->fbuf, g->fbuf + nx * ny))) { gpu_err("cpic_get_E", rc); return -1; }
-	fill_view(f->E[X], g->fbuf, nx, ny, E_NG_SOUTH);
-	fill_view(f->E[Y], g->fbuf + nx * ny, nx, ny, E_NG_SOUTH);
+	/* E comes with its south ghost row: (ny + 1) x nx per component */
+	i64 ne = nx * (ny + E_NG_SOUTH);
+	if((rc = cpic_get_E(g->ctx, g->fbuf, g->fbuf + ne))) { gpu_err("cpic_get_E", rc); return -1; }
+	fill_view(f->E[X], g->fbuf, nx, ny + E_NG_SOUTH, 0);
+	fill_view(f->E[Y], g->fbuf + ne, nx, ny + E_NG_SOUTH, 0);
 	return 0;
 }
 
@@ -410,7 +412,7 @@ gpu_setup(sim_t *sim)
 	for(int is = 0; is < (int) sim->nspecies; is++) ntot += g->n[is];
 	g->buf = malloc(4 * (size_t) nmax * sizeof(double));
 	g->ebuf = malloc(2 * (size_t) (ntot ? ntot : 1) * sizeof(double));
-	g->fbuf = malloc(2 * (size_t) p.nx * (size_t) p.ny * sizeof(double));
+	g->fbuf = malloc(2 * (size_t) p.nx * (size_t) (p.ny + 1) * sizeof(double));
 	if(!g->buf || !g->ebuf || !g->fbuf) return 1;
 
 	for(int is = 0; is < (int) sim->nspecies; is++)

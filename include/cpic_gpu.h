@@ -208,7 +208,7 @@ CPIC_API void cpic_ensemble_destroy(cpic_ensemble_t *e);
 
 /* nsteps steps of every run.  Iteration 0 runs eagerly; then one CUDA graph
  * holding two steps of every run (each run an independent branch) is
- * captured once and relaunched, the runs' status checked every 16 steps
+ * captured once and relaunched, the runs' status checked every 4 steps
  * (a run whose tile layout is rebuilt causes one re-capture).  ms_graph:
  * CUDA-event time of the graph launches; captures: graphs captured so far
  * (either may be NULL). */
