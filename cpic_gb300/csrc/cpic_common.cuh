@@ -78,6 +78,9 @@ struct Spill {
 	int32_t *id;
 	int32_t *count;     // number of records
 	int32_t capacity;
+	// 0: x, y are positions (uploads); 1: x, y are cell index + in-cell
+	// offset in cell units, which carries a mixed-form record exactly
+	int32_t cell_units;
 };
 
 struct Grid {
@@ -347,12 +350,13 @@ void launch_spill_f64(const SpillArgs &a, cudaStream_t s);
 void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s);
 void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
-		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo);
+		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo,
+		const double *Gt);
 
 void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
 void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
-		const double *cosy, float *phi, cudaStream_t s);
+		const double *cosy, float *phi, cudaStream_t s, const float *Gt);
 } // namespace cpic

@@ -15,6 +15,7 @@
 #include "../../include/cpic_gpu.h"
 #include "cpic_common.cuh"
 #include "cpic_push.cuh"
+#include "cpic_fft.cuh"
 
 namespace cpic {
 void launch_gather_f64_tiles(const Grid &g, const StoreF64 &st, const int64_t *base,
@@ -69,6 +70,8 @@ struct cpic_ctx {
 	double2 *twx64, *twy64;
 	float2 *twx32, *twy32;
 	double *cosx, *cosy;
+	double *green64;          // Green's function, column order (FP64 form)
+	float *green32;           // same, FP32 (mixed form)
 	double *mean;             // device scalar (mixed form)
 	long long *rho_sum;       // device scalar
 	uint32_t *status;
@@ -478,9 +481,10 @@ static void free_store(cpic_ctx *c, SpeciesHost &S, bool alt)
 	}
 }
 
-static int alloc_spill(Spill &S, int32_t capacity)
+static int alloc_spill(Spill &S, int32_t capacity, int cell_units = 0)
 {
 	S.capacity = capacity;
+	S.cell_units = cell_units;
 	CK(cudaMalloc(&S.x, (size_t) capacity * sizeof(double)));
 	CK(cudaMalloc(&S.y, (size_t) capacity * sizeof(double)));
 	CK(cudaMalloc(&S.ux, (size_t) capacity * sizeof(double)));
@@ -710,13 +714,13 @@ static int field_stage_async(cpic_ctx *c)
 		CK(cudaMemsetAsync(c->rho_sum, 0, sizeof(long long), st));
 		k_rho_sum<<<grid_blocks(ng, 256, 2 * 152), 256, 0, st>>>(ng, c->rho, c->rho_sum);
 		launch_poisson_mix(c->g, c->rho, c->qinv, c->rho_sum, c->spec32, c->twx32, c->twy32,
-				c->cosx, c->cosy, c->phi32, st);
+				c->cosx, c->cosy, c->phi32, st, c->green32);
 		launch_E_mix(c->g, c->phi32, c->E32, st);
 	}
 	else
 	{
 		launch_poisson_f64(c->g, c->rho, c->qinv, c->spec64, c->twx64, c->twy64,
-				c->cosx, c->cosy, c->phi64, st, c->rho_lo, c->qinv_lo);
+				c->cosx, c->cosy, c->phi64, st, c->rho_lo, c->qinv_lo, c->green64);
 		launch_E_f64(c->g, c->phi64, c->Ex64, c->Ey64, st);
 	}
 	CK(cudaGetLastError());
@@ -865,6 +869,25 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 						cudaMemcpyHostToDevice);
 		}
 	}
+	// the Green's function once, as MFT_init tabulates it (solver.c:257-280)
+	if(c->precision == CPIC_FP64)
+	{
+		if(cudaMalloc(&c->green64, (size_t) nh * g.ny * sizeof(double)) != cudaSuccess)
+		{
+			r = CPIC_ENOMEM;
+			goto fail;
+		}
+		k_green<double><<<grid_blocks(nh * g.ny), 256>>>(g.nx, g.ny, c->cosx, c->cosy, c->green64);
+	}
+	else
+	{
+		if(cudaMalloc(&c->green32, (size_t) nh * g.ny * sizeof(float)) != cudaSuccess)
+		{
+			r = CPIC_ENOMEM;
+			goto fail;
+		}
+		k_green<float><<<grid_blocks(nh * g.ny), 256>>>(g.nx, g.ny, c->cosx, c->cosy, c->green32);
+	}
 	if(cudaDeviceSynchronize() != cudaSuccess) { r = CPIC_ECUDA; goto fail; }
 	*out = c;
 	return CPIC_OK;
@@ -890,7 +913,7 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 	cudaFree(c->rho); cudaFree(c->rho_lo); cudaFree(c->phi64); cudaFree(c->Ex64); cudaFree(c->Ey64);
 	cudaFree(c->phi32); cudaFree(c->E32); cudaFree(c->spec64); cudaFree(c->spec32);
 	cudaFree(c->twx64); cudaFree(c->twy64); cudaFree(c->twx32); cudaFree(c->twy32);
-	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->mean); cudaFree(c->rho_sum);
+	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->green64); cudaFree(c->green32); cudaFree(c->mean); cudaFree(c->rho_sum);
 	cudaFree(c->status); cudaFree(c->scratch); cudaFree(c->counter);
 	if(c->stream) cudaStreamDestroy(c->stream);
 	delete c;
@@ -957,8 +980,9 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	// room for an eighth of the species to overflow between two host checks
 	int32_t scap = (int32_t) std::max<int64_t>(65536, n / 8);
 	int r;
-	if((r = alloc_spill(S.spill[0], scap))) return r;
-	if((r = alloc_spill(S.spill[1], scap))) return r;
+	const int cu = c->precision == CPIC_MIXED ? 1 : 0;
+	if((r = alloc_spill(S.spill[0], scap, cu))) return r;
+	if((r = alloc_spill(S.spill[1], scap, cu))) return r;
 	c->nspecies++;
 
 	// staging upload in the FP64 spill layout, then a counting sort

@@ -121,10 +121,32 @@ __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, dou
 	}
 }
 
+// The Green's function G(kx, ky) = 1 / (2 (cos(2 pi kx/nx) + cos(2 pi
+// ky/ny)) - 4), G(0, 0) = 0 (solver.c:269-280), stored once per context in
+// column order Gt[kx * ny + ky] (the order k_cols reads it), as type T.
+// Evaluated in FP64 from the same cosine tables and with the same
+// operations as k_cols's fallback below, so both give identical values.
+template <typename T>
+__global__ void k_green(int nx, int ny, const double *cosx, const double *cosy, T *Gt)
+{
+	int nh = nx / 2 + 1;
+	int64_t total = (int64_t) nh * ny;
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
+			i += (int64_t) gridDim.x * blockDim.x)
+	{
+		int kx = (int) (i / ny), row = (int) (i - (int64_t) kx * ny);
+		double G = (kx == 0 && row == 0) ? 0.0 : 1.0 / (2.0 * (cosx[kx] + cosy[row]) - 4.0);
+		Gt[i] = (T) G;
+	}
+}
+
 // Columns [c0, c0 + cb) of spec: FFT along y, multiply by G, inverse FFT.
+// Gt: the precomputed Green's function (k_green), or null to evaluate it
+// from the cosine tables (FP64 division per element: slow on a GPU with
+// few FP64 units, kept for callers without the table).
 template <typename T>
 __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *spec,
-		const typename Cx<T>::t *tw, const double *cosx, const double *cosy)
+		const typename Cx<T>::t *tw, const double *cosx, const double *cosy, const T *Gt)
 {
 	typedef typename Cx<T>::t C;
 	extern __shared__ unsigned char smem_raw[];
@@ -140,15 +162,30 @@ __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *sp
 	}
 	__syncthreads();
 	C *X = fft_smem<C>(a, b, ny, log2ny, ncol, -1, tw);
-	for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
+	if(Gt)
 	{
-		int c = idx / ny, row = idx - c * ny;
-		int kx = c0 + c;
-		double G = (kx == 0 && row == 0) ? 0.0 : 1.0 / (2.0 * (cosx[kx] + cosy[row]) - 4.0);
-		C v = X[idx];
-		v.x = v.x * (T) G;
-		v.y = v.y * (T) G;
-		X[idx] = v;
+		const T *Gc = Gt + (size_t) c0 * ny;    // columns are contiguous
+		for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
+		{
+			T G = Gc[idx];
+			C v = X[idx];
+			v.x = v.x * G;
+			v.y = v.y * G;
+			X[idx] = v;
+		}
+	}
+	else
+	{
+		for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
+		{
+			int c = idx / ny, row = idx - c * ny;
+			int kx = c0 + c;
+			double G = (kx == 0 && row == 0) ? 0.0 : 1.0 / (2.0 * (cosx[kx] + cosy[row]) - 4.0);
+			C v = X[idx];
+			v.x = v.x * (T) G;
+			v.y = v.y * (T) G;
+			X[idx] = v;
+		}
 	}
 	__syncthreads();
 	C *Y = (X == a) ? b : a;
@@ -241,7 +278,7 @@ template <typename T>
 static void poisson_launch(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		typename Cx<T>::t *spec, const typename Cx<T>::t *twx, const typename Cx<T>::t *twy,
 		const double *cosx, const double *cosy, T *phi, cudaStream_t s,
-		const long long *rho_lo = nullptr, double qinv_lo = 0.0)
+		const long long *rho_lo = nullptr, double qinv_lo = 0.0, const T *Gt = nullptr)
 {
 	typedef typename Cx<T>::t C;
 	int log2nx = 0, log2ny = 0;
@@ -258,7 +295,8 @@ static void poisson_launch(const Grid &g, const long long *rho, double qinv, con
 	if(cb > nh) cb = nh;
 	size_t csm = 2 * (size_t) cb * g.ny * sizeof(C);
 	int cthreads = 512;
-	k_cols<T><<<(nh + cb - 1) / cb, cthreads, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy);
+	k_cols<T><<<(nh + cb - 1) / cb, cthreads, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy,
+			Gt);
 	k_rows_inv<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, phi);
 }
 
@@ -281,7 +319,8 @@ static void poisson_launch_real(const Grid &g, const T *in, typename Cx<T>::t *s
 	if(cb < 1) cb = 1;
 	if(cb > nh) cb = nh;
 	size_t csm = 2 * (size_t) cb * g.ny * sizeof(C);
-	k_cols<T><<<(nh + cb - 1) / cb, 512, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy);
+	k_cols<T><<<(nh + cb - 1) / cb, 512, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy,
+			nullptr);
 	k_rows_inv<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, out);
 }
 

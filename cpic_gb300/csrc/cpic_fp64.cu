@@ -88,7 +88,8 @@ void launch_spill_f64(const SpillArgs &a, cudaStream_t s)
 
 void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
-		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo)
+		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo,
+		const double *Gt)
 {
 	static bool init = false;
 	if(!init)
@@ -98,7 +99,8 @@ void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		cudaFuncSetAttribute(k_rows_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 		init = true;
 	}
-	poisson_launch<double>(g, rho, qinv, nullptr, spec, twx, twy, cosx, cosy, phi, s, rho_lo, qinv_lo);
+	poisson_launch<double>(g, rho, qinv, nullptr, spec, twx, twy, cosx, cosy, phi, s, rho_lo, qinv_lo,
+			Gt);
 }
 
 } // namespace cpic

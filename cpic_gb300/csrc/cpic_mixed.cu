@@ -89,7 +89,7 @@ void launch_spill_mix(const SpillArgs &a, cudaStream_t s)
 
 void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
-		const double *cosy, float *phi, cudaStream_t s)
+		const double *cosy, float *phi, cudaStream_t s, const float *Gt)
 {
 	static bool init = false;
 	if(!init)
@@ -99,7 +99,7 @@ void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const 
 		cudaFuncSetAttribute(k_rows_inv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 		init = true;
 	}
-	poisson_launch<float>(g, rho, qinv, mean, spec, twx, twy, cosx, cosy, phi, s);
+	poisson_launch<float>(g, rho, qinv, mean, spec, twx, twy, cosx, cosy, phi, s, nullptr, 0.0, Gt);
 }
 
 } // namespace cpic

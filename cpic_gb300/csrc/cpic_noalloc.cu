@@ -147,7 +147,7 @@ cpic_poisson_noalloc(const double *rho, double *phi, int64_t nx, int64_t ny, voi
 	if(cb < 1) cb = 1;
 	if(cb > nh) cb = nh;
 	k_cols<double><<<(nh + cb - 1) / cb, 512, 2 * (size_t) cb * nyi * sizeof(double2), s>>>(
-			nxi, nyi, log2ny, cb, spec, twy, cosx, cosy);
+			nxi, nyi, log2ny, cb, spec, twy, cosx, cosy, nullptr);
 	k_rows_inv<double><<<nyi / 2, rthreads, 2 * (size_t) nxi * sizeof(double2), s>>>(
 			nxi, log2nx, nyi, spec, twx, phi);
 	return cudaGetLastError() == cudaSuccess ? CPIC_OK : CPIC_ECUDA;

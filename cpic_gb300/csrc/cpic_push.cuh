@@ -326,6 +326,12 @@ struct F64 {
 		x = r.x; y = r.y; ux = r.ux; uy = r.uy;
 	}
 
+	static __device__ __forceinline__ void to_spill_rec(const Rec &r, const Grid &g,
+			double &x, double &y, double &ux, double &uy)
+	{
+		to_spill_vals(r, g, x, y, ux, uy);
+	}
+
 	static __device__ __forceinline__ int cell_of(const Rec &r, const Grid &g, int &cx, int &cy)
 	{
 		double w[4];
@@ -597,7 +603,8 @@ struct Mix {
 	static __device__ __forceinline__ Rec from_spill(const Spill &S, int64_t k, const Grid &g)
 	{
 		Rec r;
-		double px = S.x[k] * g.idx, py = S.y[k] * g.idy;
+		double px = S.cell_units ? S.x[k] : S.x[k] * g.idx;
+		double py = S.cell_units ? S.y[k] : S.y[k] * g.idy;
 		double fx = floor(px), fy = floor(py);
 		int cx = wrap2((int) fx, g.nx), cy = wrap2((int) fy, g.ny);
 		float ox = (float) (px - fx), oy = (float) (py - fy);
@@ -616,6 +623,17 @@ struct Mix {
 		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
 		x = ((double) cx + (double) r.ox) * g.dx;
 		y = ((double) cy + (double) r.oy) * g.dy;
+		ux = r.ux; uy = r.uy;
+	}
+
+	// A spill record in cell units (cell_units lists): cx + ox is exact in
+	// FP64, so a record that passes through the spill list is unchanged.
+	static __device__ __forceinline__ void to_spill_rec(const Rec &r, const Grid &g,
+			double &x, double &y, double &ux, double &uy)
+	{
+		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
+		x = (double) cx + (double) r.ox;
+		y = (double) cy + (double) r.oy;
 		ux = r.ux; uy = r.uy;
 	}
 
@@ -785,7 +803,7 @@ k_push(const PushArgs a)
 				else
 				{
 					double x, y, ux, uy;
-					F::to_spill_vals(rec[k], g, x, y, ux, uy);
+					F::to_spill_rec(rec[k], g, x, y, ux, uy);
 					spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id, a.status);
 				}
 			}
@@ -838,7 +856,7 @@ k_spill(const SpillArgs sa)
 				else
 				{
 					double x, y, ux, uy;
-					F::to_spill_vals(r, g, x, y, ux, uy);
+					F::to_spill_rec(r, g, x, y, ux, uy);
 					spill_push(a.spill_out[s], x, y, ux, uy, r.id, a.status);
 				}
 			}

@@ -30,6 +30,12 @@
  * Optional config group (absent in the reference's .conf files):
  *   gpu = { precision = "fp64" | "mixed"; host_sync = 1;
  *           tile = [tx, ty]; halo = h; };
+ * and, per species, an initial state the reference's init methods
+ * (particle.c:170-175) cannot express, applied after them:
+ *   gpu_init = { method = "two stream"; v0 = 0.2; vth = 0.01; amp = 0.01;
+ *                seed = 1; };                     (cpic_init_two_stream)
+ *   gpu_init = { method = "maxwellian"; vth = 0.05; drift = [0.0, 0.0];
+ *                seed = 1; };                     (cpic_init_maxwellian)
  *
  * Limits: one MPI process (the GPU library owns the whole domain), the
  * "MFT" solver only, 2D, in-plane velocities (u_z = 0) and B along z.
@@ -349,6 +355,55 @@ sync_particles(sim_t *sim, const double *ebuf)
  * GPU context
  * --------------------------------------------------------------------- */
 
+static double
+conf_float(config_setting_t *g, const char *name, double dflt)
+{
+	double v;
+	int i;
+	if(config_setting_lookup_float(g, name, &v) == CONFIG_TRUE) return v;
+	if(config_setting_lookup_int(g, name, &i) == CONFIG_TRUE) return i;
+	return dflt;
+}
+
+/* The species' gpu_init group, if any, replaces the state the host's init
+ * method produced (same particle count; ids are kept). */
+static int
+apply_gpu_init(sim_t *sim, int is, int64_t n, double *x, double *y, double *ux, double *uy)
+{
+	config_setting_t *gi = config_setting_get_member(sim->species[is].conf, "gpu_init");
+	const char *method = NULL;
+	int seed = (int) sim->seed;
+	if(!gi) return 0;
+	if(config_setting_lookup_string(gi, "method", &method) != CONFIG_TRUE)
+	{
+		fprintf(stderr, "sim_gpu: species %d: gpu_init without a method\n", is);
+		return 1;
+	}
+	config_setting_lookup_int(gi, "seed", &seed);
+	if(!strcmp(method, "two stream"))
+		cpic_init_two_stream((uint64_t) seed, is, n, sim->L[X], sim->L[Y],
+				conf_float(gi, "v0", 0.0), conf_float(gi, "vth", 0.0),
+				conf_float(gi, "amp", 0.0), x, y, ux, uy);
+	else if(!strcmp(method, "maxwellian"))
+	{
+		double drift[2] = {0.0, 0.0};
+		config_setting_t *d = config_setting_get_member(gi, "drift");
+		if(d && config_setting_length(d) == 2)
+		{
+			drift[0] = config_setting_get_float_elem(d, 0);
+			drift[1] = config_setting_get_float_elem(d, 1);
+		}
+		cpic_init_maxwellian((uint64_t) seed, is, n, sim->L[X], sim->L[Y],
+				conf_float(gi, "vth", 0.0), drift[0], drift[1], x, y, ux, uy);
+	}
+	else
+	{
+		fprintf(stderr, "sim_gpu: species %d: unknown gpu_init method \"%s\"\n", is, method);
+		return 1;
+	}
+	return 0;
+}
+
 static int
 gpu_setup(sim_t *sim)
 {
@@ -427,6 +482,7 @@ gpu_setup(sim_t *sim)
 			return 1;
 		}
 		if(got != n) return 1;
+		if(apply_gpu_init(sim, is, n, x, y, ux, uy)) return 1;
 		rc = cpic_add_species(g->ctx, sim->species[is].q, sim->species[is].m, n, x, y, ux, uy);
 		if(rc < 0) { gpu_err("cpic_add_species", rc); return 1; }
 	}

@@ -35,9 +35,14 @@ def test_sim_entry_points_come_from_dropin(out):
     assert {"cpic_create", "cpic_pre_step", "cpic_step", "cpic_stage_plasma"} <= undefined
 
 
+CONF = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "cpic_gb300",
+                    "dropin", "conf", "two_stream_64.conf")
+
+
 @pytest.mark.parametrize("prog,conf", [("test_constant_speed_gpu", None),
                                        ("test_cyclotron_gpu", None),
-                                       ("cpic_gpu", "conf/constant-speed.conf")])
+                                       ("cpic_gpu", "conf/constant-speed.conf"),
+                                       ("cpic_gpu", CONF)])
 def test_reference_callers_reach_gpu_library(out, prog, conf):
     import torch
     if torch.cuda.is_available():

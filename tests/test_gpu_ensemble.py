@@ -34,7 +34,10 @@ def test_ensemble_equals_independent_runs(lib, prec):
     runs = [_member(*m, prec) for m in MEMBERS]
     ens = _lib.Ensemble(runs)
     ms, caps = ens.run(steps)
-    assert caps == 1
+    # cold beams bunch: some runs' tiles overflow and get rebuilt (the
+    # graph is then captured again); the spill path carries records
+    # exactly, so the results cannot depend on when that happens
+    assert caps >= 1
     for m, c in zip(MEMBERS, runs):
         ref = _member(*m, prec)
         ref.run(steps)
