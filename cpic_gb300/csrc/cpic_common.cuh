@@ -325,17 +325,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 	return false;
 }
 
-// Append a record to a spill list; false when the list is full.
+// Append a record to a spill list; false when the list is full (the count
+// then exceeds the capacity, which readers clamp and the host takes as a
+// reason to rebuild).
 __device__ __forceinline__ bool
-spill_push(const Spill &S, double x, double y, double ux, double uy, int32_t id,
-		uint32_t *status)
+spill_push(const Spill &S, double x, double y, double ux, double uy, int32_t id)
 {
 	int k = atomicAdd(S.count, 1);
 	if(k >= S.capacity)
-	{
-		set_status(status, ST_SPILL_FULL);
 		return false;
-	}
 	S.x[k] = x; S.y[k] = y; S.ux[k] = ux; S.uy[k] = uy;
 	S.id[k] = id;
 	return true;

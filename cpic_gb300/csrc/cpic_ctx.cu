@@ -684,6 +684,13 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 	for(int s = 0; s < c->nspecies; s++)
 		sa.spill_in[s] = c->sp[s].spill[cur];
 	size_t smem = push_smem(c);
+	// the spill pass first: its records go to their tiles or to the empty
+	// output list (same capacity as its input), so none can be lost; the
+	// fused kernel's own overflow then falls back to staying in its tile
+	if(c->precision == CPIC_MIXED)
+		launch_spill_mix(sa, st);
+	else
+		launch_spill_f64(sa, st);
 	if(ev0) CK(cudaEventRecord(ev0, st));
 	if(c->precision == CPIC_MIXED)
 		launch_push_mix(sa.p, c->ntiles, smem, st);
@@ -691,10 +698,6 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 		launch_push_f64(sa.p, c->ntiles, smem, st);
 	if(ev1) CK(cudaEventRecord(ev1, st));
 	CK(cudaGetLastError());
-	if(c->precision == CPIC_MIXED)
-		launch_spill_mix(sa, st);
-	else
-		launch_spill_f64(sa, st);
 	dim3 fg(c->ntiles, c->nspecies);
 	if(c->precision == CPIC_MIXED)
 		k_fixup<Mix><<<fg, 256, 0, st>>>(sa.p);

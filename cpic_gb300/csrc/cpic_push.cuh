@@ -436,22 +436,18 @@ struct Mix {
 		float dxo = 1.0f - ox, dyo = 1.0f - oy;
 		float w00 = dxo * dyo, w01 = dxo * oy, w10 = ox * dyo, w11 = ox * oy;
 		float2 e00, e01, e10, e11;
-		if(Etile)
+		const int lx = cx - tx0, ly = cy - ty0;
+		if(Etile && (unsigned) lx < (unsigned) g.tx && (unsigned) ly < (unsigned) g.ty)
 		{
 			const float2 *Et = (const float2 *) Etile;
 			int W = g.tx + 1;
-			int lx = cx - tx0, ly = cy - ty0;
-			if((unsigned) lx >= (unsigned) g.tx || (unsigned) ly >= (unsigned) g.ty)
-			{
-				o.err |= ST_RANGE;
-				lx = min(max(lx, 0), g.tx - 1);
-				ly = min(max(ly, 0), g.ty - 1);
-			}
 			const float2 *p = Et + ly * W + lx;
 			e00 = p[0]; e01 = p[W]; e10 = p[1]; e11 = p[W + 1];
 		}
 		else
 		{
+			// spill records, and particles kept outside their tile when
+			// their destination and the spill list were both full
 			int x1 = wrap2(cx + 1, g.nx), y1 = wrap2(cy + 1, g.ny);
 			e00 = a.E32[((int64_t) cy << g.lnx) + cx];
 			e01 = a.E32[((int64_t) y1 << g.lnx) + cx];
@@ -804,7 +800,11 @@ k_push(const PushArgs a)
 				{
 					double x, y, ux, uy;
 					F::to_spill_rec(rec[k], g, x, y, ux, uy);
-					spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id, a.status);
+					// spill list full too: the particle stays in this
+					// tile, outside its cell's tile (every later pass
+					// handles that), until the host rebuilds the layout
+					if(!spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id))
+						at = base + atomicAdd(&s_cursor, 1);
 				}
 			}
 			if(at >= 0)
@@ -857,7 +857,10 @@ k_spill(const SpillArgs sa)
 				{
 					double x, y, ux, uy;
 					F::to_spill_rec(r, g, x, y, ux, uy);
-					spill_push(a.spill_out[s], x, y, ux, uy, r.id, a.status);
+					// cannot fail: this pass runs first, on an empty
+					// list of the same capacity as its input
+					if(!spill_push(a.spill_out[s], x, y, ux, uy, r.id))
+						set_status(a.status, ST_SPILL_FULL);
 				}
 			}
 		}
