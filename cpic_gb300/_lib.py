@@ -81,6 +81,7 @@ SIGNATURES = [
     ("cpic_status_bits", ctypes.c_uint32, [ctypes.c_void_p]),
     ("cpic_time_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, D, D, D]),
     ("cpic_tile_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
+    ("cpic_layout_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     ("cpic_poisson_noalloc", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                             ctypes.c_int64, ctypes.c_void_p]),
     ("cpic_ensemble_create", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
@@ -278,6 +279,11 @@ class Context:
         self._check(self.lib.cpic_time_steps(self.h, n, ctypes.byref(a), ctypes.byref(b),
                                              ctypes.byref(c)), "cpic_time_steps")
         return dict(ms_total=a.value, ms_plasma=b.value, ms_field=c.value)
+
+    def layout_stats(self):
+        out = (ctypes.c_int64 * 4)()
+        self._check(self.lib.cpic_layout_stats(self.h, out), "cpic_layout_stats")
+        return dict(last_spill=out[0], rebuilds=out[1], slack_pct=out[2])
 
     def tile_info(self):
         out = (ctypes.c_int32 * 4)()

@@ -43,6 +43,7 @@ struct SpeciesHost {
 	Tiles tiles;
 	Spill spill[2];          // ping-pong: spill[cur] is the input
 	double vmax;              // largest initial |u| component
+	double wq_mult;           // mixed form: fixed-point units per weight unit
 };
 
 struct cpic_ctx {
@@ -52,9 +53,12 @@ struct cpic_ctx {
 	int precision;
 	int64_t iter;
 	bool prepared;
-	int slack_pct = 25;       // tile capacity slack, grows after overflows
+	int slack_pct;            // tile capacity slack %, grows after overflows
+	int64_t rebuilds;         // layout rebuilds forced by overflows
+	int64_t last_spill;       // overflow records seen at the last check
 	double qscale, qinv;
 	double qlo_mul, qinv_lo;  // FP64 form: remainder-word scales
+	bool wq_exact;            // mixed form: integer charge multiples
 	cudaStream_t stream;
 	int nspecies;
 	SpeciesHost sp[kMaxSpecies];
@@ -406,7 +410,7 @@ static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
 		double vq = -q / p.e0;
 		st.qfix = vq * c->qscale;
 		st.qlo_mul = c->qlo_mul;
-		st.wq_scale = st.qfix * ldexp(1.0, -kWeightBits);
+		st.wq_scale = c->wq_exact ? c->sp[s].wq_mult : st.qfix * ldexp(1.0, -kWeightBits);
 		st.dtqm2_f = (float) st.dtqm2;
 		st.tz_f = (float) st.tz;
 		st.sz_f = (float) st.sz;
@@ -636,14 +640,17 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 
 static int rebuild_if_spilled(cpic_ctx *c)
 {
+	c->last_spill = 0;
 	for(int s = 0; s < c->nspecies; s++)
 	{
 		int32_t ns = 0;
 		CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
 				cudaMemcpyDeviceToHost));
+		c->last_spill += ns;
 		if(ns > 0)
 		{
 			// a tile overflowed: more headroom from now on
+			c->rebuilds++;
 			c->slack_pct = std::min(200, 2 * c->slack_pct);
 			int r = rebuild_species(c, s, false, nullptr, 0);
 			if(r) return r;
@@ -765,6 +772,7 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 
 	cpic_ctx *c = new cpic_ctx();
 	memset((void *) c, 0, sizeof(*c));
+	c->slack_pct = 25;
 	c->p = *p;
 	c->precision = p->precision;
 	c->iter = -1;
@@ -934,6 +942,37 @@ static void update_qscale(cpic_ctx *c)
 	int k = (int) floor(62.0 - log2(bound)) - 1;
 	c->qscale = ldexp(1.0, k);
 	c->qinv = ldexp(1.0, -k);
+	// Mixed form: the deposit is integer weight units (2^-kWeightBits).
+	// When every species' charge is an integer multiple (up to 1024) of the
+	// smallest one, u, the fixed-point unit is u 2^-kWeightBits and a weight
+	// unit of species s is exactly mult_s of them: every sum is then exact,
+	// whichever path (tile accumulator, global fallback, spill list) a
+	// particle's contribution takes.  Otherwise the scale above is used and
+	// each path rounds its own sums.
+	c->wq_exact = false;
+	if(c->precision == CPIC_MIXED && c->nspecies > 0)
+	{
+		double u = INFINITY;
+		for(int s = 0; s < c->nspecies; s++)
+			if(c->sp[s].n > 0) u = std::min(u, fabs(c->sp[s].q / c->p.e0));
+		bool ok = u > 0.0 && std::isfinite(u);
+		double units = 0.0;
+		for(int s = 0; s < c->nspecies && ok; s++)
+		{
+			double r = fabs(c->sp[s].q / c->p.e0) / u;
+			double mi = nearbyint(r);
+			if(mi < 1.0 || mi > 1024.0 || fabs(r - mi) > 1e-9 * r) ok = false;
+			double vq = -c->sp[s].q / c->p.e0;
+			c->sp[s].wq_mult = vq < 0 ? -mi : mi;
+			units += (double) c->sp[s].n * mi;
+		}
+		if(ok && units * ldexp(1.0, kWeightBits) < ldexp(1.0, 61))
+		{
+			c->wq_exact = true;
+			c->qscale = ldexp(1.0, kWeightBits) / u;
+			c->qinv = u * ldexp(1.0, -kWeightBits);
+		}
+	}
 	// FP64 form: remainder word at 2^m finer resolution.  Every remainder
 	// is at most 2^(m-1) in magnitude and a node receives at most one per
 	// particle, so m = 62 - ceil(log2(N + 1)) keeps its sums below 2^62.
@@ -1376,6 +1415,16 @@ CPIC_API int cpic_time_steps(cpic_ctx_t *c, int64_t nsteps, double *ms_total, do
 	if(r) return r;
 	if((r = check_status(c))) return r;
 	return rebuild_if_spilled(c);
+}
+
+CPIC_API int cpic_layout_stats(const cpic_ctx_t *c, int64_t *out)
+{
+	if(!c || !out) return CPIC_EINVAL;
+	out[0] = c->last_spill;
+	out[1] = c->rebuilds;
+	out[2] = c->slack_pct;
+	out[3] = 0;
+	return CPIC_OK;
 }
 
 CPIC_API int cpic_tile_info(const cpic_ctx_t *c, int32_t *out)

@@ -175,6 +175,12 @@ CPIC_API int cpic_time_steps(cpic_ctx_t *ctx, int64_t nsteps, double *ms_total,
  * capacity slack in percent}. */
 CPIC_API int cpic_tile_info(const cpic_ctx_t *ctx, int32_t *out);
 
+/* Health of the tile layout, out[4]: {overflow records (particles that
+ * found no room in their destination tile) seen at the last host check,
+ * layout rebuilds forced by overflows so far, current capacity slack in
+ * percent, 0}. */
+CPIC_API int cpic_layout_stats(const cpic_ctx_t *ctx, int64_t *out);
+
 /* --- solve without allocation ------------------------------------------ */
 
 /* Largest grid side accepted by cpic_poisson_noalloc: its scratch is one
