@@ -78,7 +78,7 @@ void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 		init = true;
 	}
 	dim3 grid(ntiles, a.nspecies);
-	k_push<F64><<<grid, kPushBlock, smem, s>>>(a);
+	k_push<F64><<<grid, kPushThreads, smem, s>>>(a);
 }
 
 void launch_spill_f64(const SpillArgs &a, cudaStream_t s)

@@ -79,7 +79,7 @@ void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 		init = true;
 	}
 	dim3 grid(ntiles, a.nspecies);
-	k_push<Mix><<<grid, kPushBlock, smem, s>>>(a);
+	k_push<Mix><<<grid, kPushThreads, smem, s>>>(a);
 }
 
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s)

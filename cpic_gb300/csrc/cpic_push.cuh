@@ -540,10 +540,9 @@ struct Mix {
 	// Move the 32-bit sums into the 64-bit shadow (between barriers).
 	static __device__ __forceinline__ void fold(unsigned char *sm, int W, int T)
 	{
-		// run by the compute warps only
 		uint32_t *a32 = sh32(sm, W, T);
 		unsigned long long *a64 = sh64(sm);
-		for(int i = threadIdx.x; i < W * W; i += kPushThreads)
+		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
 		{
 			a64[i] += a32[i];
 			a32[i] = 0;
@@ -648,19 +647,8 @@ struct Mix {
 
 // ============================================================== kernels
 
-// Block shape: kPushThreads threads (kPushThreads / 32 warps) push the
-// particles, one more warp streams the chunks in (a producer that never
-// blocks the compute warps).
-constexpr int kPushBlock = kPushThreads + 32;
-
-// Barrier 1 among the compute warps only (barrier 0 is __syncthreads).
-__device__ __forceinline__ void compute_sync()
-{
-	asm volatile("bar.sync 1, %0;" :: "n"(kPushThreads) : "memory");
-}
-
 template <class F>
-__global__ void __launch_bounds__(kPushBlock, F::kMinBlocks)
+__global__ void __launch_bounds__(kPushThreads, F::kMinBlocks)
 k_push(const PushArgs a)
 {
 	// dynamic shared memory: two staged chunks, then the form's area
@@ -714,24 +702,10 @@ k_push(const PushArgs a)
 		fence_mbar_init();
 	}
 	__syncthreads();
+	if(threadIdx.x == 0 && nchunks > 0)
+		F::stage_issue(a, s, base, min(kChunk, n), stage0, &bars[0]);
 	const int lane = threadIdx.x & 31;
 
-	if(threadIdx.x >= kPushThreads)
-	{
-		// producer warp: chunk ci goes into buffer ci & 1 once the compute
-		// warps have released that buffer's previous chunk, ci - 2
-		if(lane == 0)
-			for(int ci = 0; ci < nchunks; ci++)
-			{
-				const int b = ci & 1;
-				if(ci >= 2)
-					mbar_wait_bounded(&ebars[b], ((ci - 2) >> 1) & 1, a.status);
-				fence_proxy_async_smem();
-				F::stage_issue(a, s, base + (int64_t) ci * kChunk, min(kChunk, n - ci * kChunk),
-						stage0 + b * sb, &bars[b]);
-			}
-	}
-	else
 	for(int ci = 0; ci < nchunks; ci++)
 	{
 		const int c0 = ci * kChunk;
@@ -739,14 +713,24 @@ k_push(const PushArgs a)
 		{
 			// every deposit of the previous chunks precedes the fold, and
 			// the fold precedes every later deposit
-			compute_sync();
+			__syncthreads();
 			F::fold(fsm, W, g.tx);
-			compute_sync();
+			__syncthreads();
+		}
+		// prefetch the next chunk into the other buffer once every warp
+		// has released it (its last reader was chunk ci - 1)
+		if(threadIdx.x == 0 && ci + 1 < nchunks)
+		{
+			const int b = (ci + 1) & 1;
+			if(ci >= 1)
+				mbar_wait_bounded(&ebars[b], ((ci - 1) >> 1) & 1, a.status);
+			fence_proxy_async_smem();
+			F::stage_issue(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
+					stage0 + b * sb, &bars[b]);
 		}
 		// this chunk has landed: every global read of slots below
 		// c0 + kChunk is complete, so the in-place writes below are safe
-		// (the stayer cursor never passes the end of the chunks read; the
-		// producer reads chunk ci + 1 at or above c0 + kChunk)
+		// (the stayer cursor never passes the end of the chunks read)
 		mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status);
 		const unsigned char *buf = stage0 + (ci & 1) * sb;
 		typename F::Rec rec[kPPT];
