@@ -167,6 +167,71 @@ __global__ void k_rb_scatter(const PushArgs newa, int s, Spill S, int64_t n, int
 	}
 }
 
+// Upload counting sort with block-local histograms (shared-memory atomics,
+// one global atomic per block and bin): the bins are (tile, sign of ux), so
+// inside every tile the particles moving left come first and those moving
+// right after them.  Warps then mostly hold particles leaving towards the
+// same neighbour from the first step on, as the in-place re-bin makes them
+// after a tile's population has been renewed.  Blocks take contiguous
+// ranges.  Shared memory: 2 nt (count) or 4 nt (scatter) ints.
+template <class F>
+__global__ void k_rb_count_blk(Grid g, Spill S, int64_t n, int nt, int32_t *cnt, int32_t *neg)
+{
+	extern __shared__ int32_t shb[];
+	for(int i = threadIdx.x; i < 2 * nt; i += blockDim.x) shb[i] = 0;
+	__syncthreads();
+	int64_t per = (n + gridDim.x - 1) / gridDim.x;
+	int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
+	for(int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
+	{
+		int t = TileOf<F>::get(g, S, k);
+		atomicAdd(&shb[(S.ux[k] >= 0.0 ? nt : 0) + t], 1);
+	}
+	__syncthreads();
+	for(int t = threadIdx.x; t < nt; t += blockDim.x)
+	{
+		int a = shb[t], b = shb[nt + t];
+		if(a) atomicAdd(&neg[t], a);
+		if(a + b) atomicAdd(&cnt[t], a + b);
+	}
+}
+
+template <class F>
+__global__ void k_rb_scatter_blk(const PushArgs na, int s, Spill S, int64_t n, int nt,
+		int32_t *fneg, int32_t *fpos)
+{
+	extern __shared__ int32_t shb[];
+	int32_t *bb = shb + 2 * nt;
+	const Grid &g = na.g;
+	for(int i = threadIdx.x; i < 2 * nt; i += blockDim.x) shb[i] = 0;
+	__syncthreads();
+	int64_t per = (n + gridDim.x - 1) / gridDim.x;
+	int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
+	for(int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
+	{
+		int t = TileOf<F>::get(g, S, k);
+		atomicAdd(&shb[(S.ux[k] >= 0.0 ? nt : 0) + t], 1);
+	}
+	__syncthreads();
+	for(int t = threadIdx.x; t < nt; t += blockDim.x)
+	{
+		int a = shb[t], b = shb[nt + t];
+		bb[t] = a ? atomicAdd(&fneg[t], a) : 0;
+		bb[nt + t] = b ? atomicAdd(&fpos[t], b) : 0;
+		shb[t] = 0;
+		shb[nt + t] = 0;
+	}
+	__syncthreads();
+	for(int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
+	{
+		int t = TileOf<F>::get(g, S, k);
+		int j = (S.ux[k] >= 0.0 ? nt : 0) + t;
+		int slot = bb[j] + atomicAdd(&shb[j], 1);
+		typename F::Rec r = F::from_spill(S, k, g);
+		F::store(na, s, na.tiles[s].base[t] + slot, r);
+	}
+}
+
 // Host view: FP64 state by particle id (or compacted through a counter).
 template <class F>
 __global__ void k_download(const PushArgs a, int s, double *x, double *y, double *ux,
@@ -528,6 +593,10 @@ static void launch_rb_count(const Grid &g, const Spill &S, int64_t cnt, int32_t 
 		k_rb_count<F><<<grid_blocks(cnt), 256, 0, st>>>(g, S, cnt, newcnt);
 }
 
+// Largest tile count of the block-local upload sort (its scatter keeps
+// 4 ints per tile in shared memory: 128 KB).
+constexpr int kBlkSortMaxTiles = 8192;
+
 // Counting-sort rebuild of species s: its tiles (unless `fresh`), its
 // current spill input and an optional staging list are merged into a new
 // layout whose tile capacities follow the new counts.
@@ -542,7 +611,7 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	CK(cudaStreamSynchronize(st));
 	if(nspill > spin.capacity) nspill = spin.capacity;
 
-	int32_t *newcnt = nullptr, *fill = nullptr;
+	int32_t *newcnt = nullptr, *fill = nullptr, *negcnt = nullptr;
 	CK(cudaMalloc(&newcnt, nt * sizeof(int32_t)));
 	CK(cudaMalloc(&fill, nt * sizeof(int32_t)));
 	if(fresh)
@@ -550,7 +619,31 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	else
 		CK(cudaMemcpyAsync(newcnt, S.tiles.cnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
 	bool mix = c->precision == CPIC_MIXED;
-	if(mix)
+	// the upload of a species: block-local counting sort by (tile, sign of ux)
+	const bool blk = fresh && staging && nspill == 0 && nstage > 0 && nt <= kBlkSortMaxTiles;
+	const int blk_blocks = (int) std::min<int64_t>(152 * 8, (nstage + 4095) / 4096);
+	if(blk)
+	{
+		static bool attr = false;
+		if(!attr)
+		{
+			const int mx = 4 * kBlkSortMaxTiles * (int) sizeof(int32_t);
+			cudaFuncSetAttribute(k_rb_count_blk<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			cudaFuncSetAttribute(k_rb_count_blk<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			cudaFuncSetAttribute(k_rb_scatter_blk<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			cudaFuncSetAttribute(k_rb_scatter_blk<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			attr = true;
+		}
+		CK(cudaMalloc(&negcnt, nt * sizeof(int32_t)));
+		CK(cudaMemsetAsync(negcnt, 0, nt * sizeof(int32_t), st));
+		if(mix)
+			k_rb_count_blk<Mix><<<blk_blocks, 512, 2 * nt * sizeof(int32_t), st>>>(c->g, *staging,
+					nstage, nt, newcnt, negcnt);
+		else
+			k_rb_count_blk<F64><<<blk_blocks, 512, 2 * nt * sizeof(int32_t), st>>>(c->g, *staging,
+					nstage, nt, newcnt, negcnt);
+	}
+	else if(mix)
 	{
 		launch_rb_count<Mix>(c->g, spin, nspill, newcnt, st);
 		if(staging) launch_rb_count<Mix>(c->g, *staging, nstage, newcnt, st);
@@ -612,7 +705,24 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 		if(mix) launch_rb_copy<Mix>(olda, newa, s, nt, st);
 		else launch_rb_copy<F64>(olda, newa, s, nt, st);
 	}
-	if(mix)
+	if(blk)
+	{
+		// left movers from slot 0, right movers after all of them
+		int32_t *fpos = nullptr;
+		CK(cudaMalloc(&fpos, nt * sizeof(int32_t)));
+		CK(cudaMemcpyAsync(fpos, negcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+		size_t sm = 4 * (size_t) nt * sizeof(int32_t);
+		if(mix)
+			k_rb_scatter_blk<Mix><<<blk_blocks, 512, sm, st>>>(newa, s, *staging, nstage, nt, fill,
+					fpos);
+		else
+			k_rb_scatter_blk<F64><<<blk_blocks, 512, sm, st>>>(newa, s, *staging, nstage, nt, fill,
+					fpos);
+		CK(cudaStreamSynchronize(st));
+		cudaFree(fpos);
+		cudaFree(negcnt);
+	}
+	else if(mix)
 	{
 		launch_rb_scatter<Mix>(newa, s, spin, nspill, fill, st);
 		if(staging) launch_rb_scatter<Mix>(newa, s, *staging, nstage, fill, st);
