@@ -422,7 +422,7 @@ struct Mix {
 	// rounded integer in the low mantissa bits.
 	static __device__ __forceinline__ uint32_t wfix(float w)
 	{
-		float f = w * (float) (1 << kWeightBits) + 8388608.0f;
+		float f = __fmaf_rn(w, (float) (1 << kWeightBits), 8388608.0f);
 		return __float_as_uint(f) - 0x4B000000u;
 	}
 
@@ -435,10 +435,16 @@ struct Mix {
 		const SpeciesStep &sp = a.sp[s];
 		Out o;
 		o.err = 0;
+		// Every floating-point operation below is an explicit-rounding
+		// intrinsic: the fused kernel and the spill pass compile this
+		// function separately, and the compiler may not contract or
+		// reassociate differently in the two, so a particle gets the same
+		// result on either path.
 		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
 		float ox = r.ox, oy = r.oy;
-		float dxo = 1.0f - ox, dyo = 1.0f - oy;
-		float w00 = dxo * dyo, w01 = dxo * oy, w10 = ox * dyo, w11 = ox * oy;
+		float dxo = __fsub_rn(1.0f, ox), dyo = __fsub_rn(1.0f, oy);
+		float w00 = __fmul_rn(dxo, dyo), w01 = __fmul_rn(dxo, oy);
+		float w10 = __fmul_rn(ox, dyo), w11 = __fmul_rn(ox, oy);
 		float2 e00, e01, e10, e11;
 		const int lx = cx - tx0, ly = cy - ty0;
 		if(Etile && (unsigned) lx < (unsigned) g.tx && (unsigned) ly < (unsigned) g.ty)
@@ -458,17 +464,20 @@ struct Mix {
 			e10 = a.E32[((int64_t) cy << g.lnx) + x1];
 			e11 = a.E32[((int64_t) y1 << g.lnx) + x1];
 		}
-		float ex = w00 * e00.x + w01 * e01.x + w10 * e10.x + w11 * e11.x;
-		float ey = w00 * e00.y + w01 * e01.y + w10 * e10.y + w11 * e11.y;
+		float ex = __fmaf_rn(w11, e11.x, __fmaf_rn(w10, e10.x, __fmaf_rn(w01, e01.x,
+				__fmul_rn(w00, e00.x))));
+		float ey = __fmaf_rn(w11, e11.y, __fmaf_rn(w10, e10.y, __fmaf_rn(w01, e01.y,
+				__fmul_rn(w00, e00.y))));
 
 		// Boris with B along z (same structure as the FP64 form)
 		float dtqm2 = sp.dtqm2_f;
-		float vmx = r.ux + dtqm2 * ex;
-		float vmy = r.uy + dtqm2 * ey;
-		float vpx = vmx + vmy * sp.tz_f;
-		float vpy = vmy - vmx * sp.tz_f;
-		float ux = vmx + vpy * sp.sz_f + dtqm2 * ex;
-		float uy = vmy - vpx * sp.sz_f + dtqm2 * ey;
+		float hx = __fmul_rn(dtqm2, ex), hy = __fmul_rn(dtqm2, ey);
+		float vmx = __fadd_rn(r.ux, hx);
+		float vmy = __fadd_rn(r.uy, hy);
+		float vpx = __fmaf_rn(vmy, sp.tz_f, vmx);
+		float vpy = __fmaf_rn(-vmx, sp.tz_f, vmy);
+		float ux = __fadd_rn(__fmaf_rn(vpy, sp.sz_f, vmx), hx);
+		float uy = __fadd_rn(__fmaf_rn(-vpx, sp.sz_f, vmy), hy);
 		if(fabsf(ux) > sp.umax_x_f || fabsf(uy) > sp.umax_y_f)
 			o.err |= ST_UMAX;
 		if(!isfinite(ux) || !isfinite(uy))
@@ -479,23 +488,23 @@ struct Mix {
 		int sx = 0, sy = 0;
 		if(a.iter != 0)
 		{
-			ox += ux * a.cdx_f;
-			oy += uy * a.cdy_f;
+			ox = __fmaf_rn(ux, a.cdx_f, ox);
+			oy = __fmaf_rn(uy, a.cdy_f, oy);
 			float fx = floorf(ox), fy = floorf(oy);
-			ox -= fx; oy -= fy;
+			ox = __fsub_rn(ox, fx); oy = __fsub_rn(oy, fy);
 			sx = (int) fx; sy = (int) fy;
-			if(ox >= 1.0f) { ox -= 1.0f; sx += 1; }
-			if(oy >= 1.0f) { oy -= 1.0f; sy += 1; }
+			if(ox >= 1.0f) { ox = __fsub_rn(ox, 1.0f); sx += 1; }
+			if(oy >= 1.0f) { oy = __fsub_rn(oy, 1.0f); sy += 1; }
 		}
 		int ncx = wrap2(cx + sx, g.nx), ncy = wrap2(cy + sy, g.ny);
 		r.cell = (ncy << g.lnx) + ncx;
 		r.ox = ox; r.oy = oy; r.ux = ux; r.uy = uy;
 
-		dxo = 1.0f - ox; dyo = 1.0f - oy;
-		o.wq[0] = wfix(dxo * dyo);
-		o.wq[1] = wfix(dxo * oy);
-		o.wq[2] = wfix(ox * dyo);
-		o.wq[3] = wfix(ox * oy);
+		dxo = __fsub_rn(1.0f, ox); dyo = __fsub_rn(1.0f, oy);
+		o.wq[0] = wfix(__fmul_rn(dxo, dyo));
+		o.wq[1] = wfix(__fmul_rn(dxo, oy));
+		o.wq[2] = wfix(__fmul_rn(ox, dyo));
+		o.wq[3] = wfix(__fmul_rn(ox, oy));
 		o.dest = tile_of(g, ncx, ncy);
 		if(Etile)
 		{
