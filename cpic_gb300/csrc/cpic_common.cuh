@@ -128,6 +128,20 @@ struct SpillArgs {
 	Spill spill_in[kMaxSpecies];
 };
 
+// The arguments of species sp moved to index 0 (the fused kernel is
+// launched once per species and reads index 0 only).
+inline PushArgs species_args(const PushArgs &a, int sp)
+{
+	PushArgs b = a;
+	b.nspecies = 1;
+	b.sp[0] = a.sp[sp];
+	b.tiles[0] = a.tiles[sp];
+	b.f64[0] = a.f64[sp];
+	b.mix[0] = a.mix[sp];
+	b.spill_out[0] = a.spill_out[sp];
+	return b;
+}
+
 // ---------------------------------------------------------------- helpers
 
 // Periodic wrap for a power-of-two extent (any sign of i).

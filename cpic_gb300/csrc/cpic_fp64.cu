@@ -77,8 +77,8 @@ void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 				cudaSharedmemCarveoutMaxShared);
 		init = true;
 	}
-	dim3 grid(ntiles, a.nspecies);
-	k_push<F64><<<grid, kPushThreads, smem, s>>>(a);
+	for(int sp = 0; sp < a.nspecies; sp++)
+		k_push<F64><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
 }
 
 void launch_spill_f64(const SpillArgs &a, cudaStream_t s)

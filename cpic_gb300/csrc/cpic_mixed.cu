@@ -78,8 +78,8 @@ void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 				cudaSharedmemCarveoutMaxShared);
 		init = true;
 	}
-	dim3 grid(ntiles, a.nspecies);
-	k_push<Mix><<<grid, kPushThreads, smem, s>>>(a);
+	for(int sp = 0; sp < a.nspecies; sp++)
+		k_push<Mix><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
 }
 
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s)

@@ -670,7 +670,9 @@ k_push(const PushArgs a)
 	__shared__ int64_t s_nbase[9];
 	__shared__ int32_t s_ncap[9];
 	const Grid &g = a.g;
-	const int s = blockIdx.y;
+	// one launch per species, its data at index 0: every parameter access
+	// has a fixed offset (no indexed constant loads in the particle loop)
+	const int s = 0;
 	const int t = blockIdx.x;
 	const Tiles &T = a.tiles[s];
 	const int H = g.halo;
@@ -680,9 +682,11 @@ k_push(const PushArgs a)
 	const bool ids = a.mix[s].id != nullptr;
 	const size_t sb = F::stage_bytes(ids);
 	// bulk-copy destinations need 16-byte alignment; the host adds 128
-	// bytes of slack for this round-up
-	unsigned char *stage0 = reinterpret_cast<unsigned char *>(
-			(reinterpret_cast<uintptr_t>(smem) + 127) & ~(uintptr_t) 127);
+	// bytes of slack for this round-up.  An offset from smem (not a pointer
+	// rebuilt from an integer) keeps every derived pointer in the shared
+	// space, so accesses compile to shared-memory loads and atomics.
+	unsigned char *stage0 = smem
+		+ ((128u - (unsigned) (reinterpret_cast<uintptr_t>(smem) & 127u)) & 127u);
 	unsigned char *fsm = stage0 + 2 * sb;
 
 	F::clear(fsm, W, g.tx);
