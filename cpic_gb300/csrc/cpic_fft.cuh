@@ -289,8 +289,9 @@ static void poisson_launch(const Grid &g, const long long *rho, double qinv, con
 	k_rows_fwd<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, rho, qinv, mean, spec, twx,
 			rho_lo, qinv_lo);
 	int nh = g.nx / 2 + 1;
-	// columns per block: fill up to 128 KB of shared memory (two buffers)
-	int cb = (int) ((128 * 1024) / (2 * (size_t) g.ny * sizeof(C)));
+	// columns per block: up to 64 KB of shared memory (two buffers), so
+	// that several blocks share an SM
+	int cb = (int) ((64 * 1024) / (2 * (size_t) g.ny * sizeof(C)));
 	if(cb < 1) cb = 1;
 	if(cb > nh) cb = nh;
 	size_t csm = 2 * (size_t) cb * g.ny * sizeof(C);
@@ -315,7 +316,7 @@ static void poisson_launch_real(const Grid &g, const T *in, typename Cx<T>::t *s
 	size_t rsm = 2 * (size_t) g.nx * sizeof(C);
 	k_rows_fwd_real<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, in, spec, twx);
 	int nh = g.nx / 2 + 1;
-	int cb = (int) ((128 * 1024) / (2 * (size_t) g.ny * sizeof(C)));
+	int cb = (int) ((64 * 1024) / (2 * (size_t) g.ny * sizeof(C)));
 	if(cb < 1) cb = 1;
 	if(cb > nh) cb = nh;
 	size_t csm = 2 * (size_t) cb * g.ny * sizeof(C);
