@@ -82,6 +82,7 @@ struct cpic_ctx {
 	double *scratch;          // FP64 scratch for host views / partial sums
 	size_t scratch_n;
 	int32_t *counter;         // device scalar
+	unsigned long long *counter_pair;  // two device scalars (upload check)
 };
 
 // ------------------------------------------------------------- kernels
@@ -232,10 +233,46 @@ __global__ void k_rb_scatter_blk(const PushArgs na, int s, Spill S, int64_t n, i
 	}
 }
 
-// Host view: FP64 state by particle id (or compacted through a counter).
+// Upload check, numbering and Y wrap of a staged species.  out[0]: any
+// invalid record (x outside [0, Lx], non-finite y, ux, uy); out[1]: the
+// largest |ux|, |uy| as the bit pattern of a non-negative double.
+__global__ void k_upload_check(int64_t n, Spill S, double Lx, double Ly, unsigned long long *out)
+{
+	unsigned long long bad = 0;
+	double vm = 0.0;
+	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+			i += (int64_t) gridDim.x * blockDim.x)
+	{
+		double x = S.x[i], y = S.y[i], u = S.ux[i], v = S.uy[i];
+		if(!(x >= 0.0 && x <= Lx) || !isfinite(y) || !isfinite(u) || !isfinite(v))
+			bad = 1;
+		else
+		{
+			vm = fmax(vm, fmax(fabs(u), fabs(v)));
+			// one periodic wrap in Y, as the initial global exchange does
+			// (sim_pre_step -> comm_plasma(sim, 1), comm_plasma.c:1087-1112)
+			if(y >= Ly) S.y[i] = y - Ly;
+			else if(y < 0.0) S.y[i] = y + Ly;
+		}
+		S.id[i] = (int32_t) i;
+	}
+	for(int o = 16; o > 0; o >>= 1)
+	{
+		bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+		vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+	}
+	if((threadIdx.x & 31) == 0)
+	{
+		if(bad) atomicOr(&out[0], 1ULL);
+		atomicMax(&out[1], (unsigned long long) __double_as_longlong(vm));
+	}
+}
+
+// Host view: FP64 state by particle id, or (prefix non-null) in store
+// order, tile t's particles from prefix[t] on.
 template <class F>
 __global__ void k_download(const PushArgs a, int s, double *x, double *y, double *ux,
-		double *uy, int32_t *counter, int by_id)
+		double *uy, const int64_t *prefix)
 {
 	int t = blockIdx.x;
 	int n = a.tiles[s].cnt[t];
@@ -245,7 +282,7 @@ __global__ void k_download(const PushArgs a, int s, double *x, double *y, double
 		typename F::Rec r = F::load(a, s, b + i);
 		double px, py, pu, pv;
 		F::to_spill_vals(r, a.g, px, py, pu, pv);
-		int64_t dst = by_id ? r.id : atomicAdd(counter, 1);
+		int64_t dst = prefix ? prefix[t] + i : (int64_t) r.id;
 		x[dst] = px; y[dst] = py; ux[dst] = pu; uy[dst] = pv;
 	}
 }
@@ -392,20 +429,6 @@ __global__ void k_iota(int64_t n, int32_t *id)
 	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
 			i += (int64_t) gridDim.x * blockDim.x)
 		id[i] = (int32_t) i;
-}
-
-// Y wrap of the initial global exchange (sim_pre_step -> comm_plasma(sim,
-// 1), src/comm_plasma.c:1087-1112): one periodic wrap in Y.
-__global__ void k_wrap_y(int64_t n, double *y, double Ly)
-{
-	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
-			i += (int64_t) gridDim.x * blockDim.x)
-	{
-		double v = y[i];
-		if(v >= Ly) v -= Ly;
-		else if(v < 0.0) v += Ly;
-		y[i] = v;
-	}
 }
 
 // ------------------------------------------------------------- helpers
@@ -937,6 +960,7 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	AL(c->mean, sizeof(double));
 	AL(c->rho_sum, sizeof(long long));
 	AL(c->counter, sizeof(int32_t));
+	AL(c->counter_pair, 2 * sizeof(unsigned long long));
 	if(c->precision == CPIC_FP64)
 	{
 		AL(c->phi64, ng * sizeof(double));
@@ -1035,7 +1059,7 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 	cudaFree(c->phi32); cudaFree(c->E32); cudaFree(c->spec64); cudaFree(c->spec32);
 	cudaFree(c->twx64); cudaFree(c->twy64); cudaFree(c->twx32); cudaFree(c->twy32);
 	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->green64); cudaFree(c->green32); cudaFree(c->mean); cudaFree(c->rho_sum);
-	cudaFree(c->status); cudaFree(c->scratch); cudaFree(c->counter);
+	cudaFree(c->status); cudaFree(c->scratch); cudaFree(c->counter); cudaFree(c->counter_pair);
 	if(c->stream) cudaStreamDestroy(c->stream);
 	delete c;
 }
@@ -1101,24 +1125,41 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 		return CPIC_EINVAL;
 	if(n > 0 && (!x || !y || !ux || !uy)) return CPIC_EINVAL;
 	if(c->prepared) return CPIC_ESTATE;
+	int r;
+	cudaStream_t st = c->stream;
+
+	// staging upload in the FP64 spill layout, checked on the device in one
+	// pass that also numbers the particles and wraps Y: x in [0, Lx] (the
+	// reference's global exchange never wraps X, comm_plasma.c:826-870),
+	// finite y, ux, uy; largest |u| component for the halo
+	Spill stg;
+	memset(&stg, 0, sizeof(stg));
+	if((r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1)))) return r;
+	double vmax = 0.0;
+	if(n > 0)
+	{
+		CK(cudaMemcpyAsync(stg.x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.y, y, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.ux, ux, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		CK(cudaMemcpyAsync(stg.uy, uy, n * sizeof(double), cudaMemcpyHostToDevice, st));
+		unsigned long long *chk = reinterpret_cast<unsigned long long *>(c->counter_pair);
+		CK(cudaMemsetAsync(chk, 0, 2 * sizeof(unsigned long long), st));
+		k_upload_check<<<grid_blocks(n, 256, 8 * 152), 256, 0, st>>>(n, stg, c->p.Lx, c->p.Ly, chk);
+		unsigned long long h[2];
+		CK(cudaMemcpyAsync(h, chk, sizeof(h), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		if(h[0])
+		{
+			free_spill(stg);
+			return CPIC_EINVAL;
+		}
+		memcpy(&vmax, &h[1], sizeof(double));
+	}
+
 	int s = c->nspecies;
 	SpeciesHost &S = c->sp[s];
 	memset((void *) &S, 0, sizeof(S));
 	S.q = q; S.m = m; S.n = n;
-	// comm_plasma's global exchange never wraps X (comm_plasma.c:826-870);
-	// checked on all host threads (hundreds of millions of particles)
-	int bad = 0;
-	double vmax = 0.0;
-	const double Lx = c->p.Lx;
-	#pragma omp parallel for schedule(static) reduction(max: vmax) reduction(|: bad)
-	for(int64_t i = 0; i < n; i++)
-	{
-		if(!(x[i] >= 0.0 && x[i] <= Lx) || !std::isfinite(y[i])
-				|| !std::isfinite(ux[i]) || !std::isfinite(uy[i]))
-			bad |= 1;
-		vmax = std::max(vmax, std::max(fabs(ux[i]), fabs(uy[i])));
-	}
-	if(bad) return CPIC_EINVAL;
 	S.vmax = vmax;
 	int nt = c->ntiles;
 	CK(cudaMalloc(&S.tiles.base, nt * sizeof(int64_t)));
@@ -1131,26 +1172,12 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	CK(cudaMemset(S.tiles.stay, 0, nt * sizeof(int32_t)));
 	// room for an eighth of the species to overflow between two host checks
 	int32_t scap = (int32_t) std::max<int64_t>(65536, n / 8);
-	int r;
 	const int cu = c->precision == CPIC_MIXED ? 1 : 0;
 	if((r = alloc_spill(S.spill[0], scap, cu))) return r;
 	if((r = alloc_spill(S.spill[1], scap, cu))) return r;
 	c->nspecies++;
 
-	// staging upload in the FP64 spill layout, then a counting sort
-	Spill stg;
-	memset(&stg, 0, sizeof(stg));
-	if((r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1)))) return r;
-	cudaStream_t st = c->stream;
-	if(n > 0)
-	{
-		CK(cudaMemcpyAsync(stg.x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
-		CK(cudaMemcpyAsync(stg.y, y, n * sizeof(double), cudaMemcpyHostToDevice, st));
-		CK(cudaMemcpyAsync(stg.ux, ux, n * sizeof(double), cudaMemcpyHostToDevice, st));
-		CK(cudaMemcpyAsync(stg.uy, uy, n * sizeof(double), cudaMemcpyHostToDevice, st));
-		k_iota<<<grid_blocks(n), 256, 0, st>>>(n, stg.id);
-		k_wrap_y<<<grid_blocks(n), 256, 0, st>>>(n, stg.y, c->p.Ly);
-	}
+	// counting sort of the staged particles into the tiles
 	update_qscale(c);
 	r = rebuild_species(c, s, true, &stg, n);
 	free_spill(stg);
@@ -1247,19 +1274,31 @@ CPIC_API int cpic_get_particles(cpic_ctx_t *c, int s, double *x, double *y, doub
 {
 	if(!c || s < 0 || s >= c->nspecies) return CPIC_EINVAL;
 	int64_t n = c->sp[s].n;
-	int r = ensure_scratch(c, 4 * (size_t) std::max<int64_t>(n, 1));
+	int nt = c->ntiles;
+	// scratch: the four FP64 columns, then the per-tile prefix (store order)
+	int r = ensure_scratch(c, 4 * (size_t) std::max<int64_t>(n, 1) + nt);
 	if(r) return r;
 	cudaStream_t st = c->stream;
 	double *d = c->scratch;
 	bool by_id = c->precision == CPIC_FP64 || c->p.track_ids;
-	CK(cudaMemsetAsync(c->counter, 0, sizeof(int32_t), st));
+	int64_t *prefix = nullptr;
+	if(!by_id)
+	{
+		std::vector<int32_t> cnt(nt);
+		std::vector<int64_t> pre(nt);
+		CK(cudaMemcpyAsync(cnt.data(), c->sp[s].tiles.cnt, nt * sizeof(int32_t),
+				cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		int64_t acc = 0;
+		for(int t = 0; t < nt; t++) { pre[t] = acc; acc += cnt[t]; }
+		prefix = reinterpret_cast<int64_t *>(d + 4 * std::max<int64_t>(n, 1));
+		CK(cudaMemcpyAsync(prefix, pre.data(), nt * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+	}
 	PushArgs a = make_args(c, c->spill_cur);
 	if(c->precision == CPIC_MIXED)
-		k_download<Mix><<<c->ntiles, 256, 0, st>>>(a, s, d, d + n, d + 2 * n, d + 3 * n,
-				c->counter, by_id);
+		k_download<Mix><<<c->ntiles, 256, 0, st>>>(a, s, d, d + n, d + 2 * n, d + 3 * n, prefix);
 	else
-		k_download<F64><<<c->ntiles, 256, 0, st>>>(a, s, d, d + n, d + 2 * n, d + 3 * n,
-				c->counter, by_id);
+		k_download<F64><<<c->ntiles, 256, 0, st>>>(a, s, d, d + n, d + 2 * n, d + 3 * n, prefix);
 	CK(cudaGetLastError());
 	double *outs[4] = {x, y, ux, uy};
 	for(int k = 0; k < 4; k++)

@@ -277,3 +277,40 @@ def test_mixed_form_independent_of_rebuild_schedule(lib):
         assert np.array_equal(u, v)
     assert np.array_equal(a.rho(), b.rho())
     assert a.field_energy() == b.field_energy()
+
+
+@pytest.mark.parametrize("prec", [_lib.FP64, _lib.MIXED], ids=["fp64", "mixed"])
+def test_invalid_uploads_are_rejected(lib, prec):
+    """cpic_add_species refuses positions outside [0, Lx] in X and
+    non-finite state (the reference aborts on them), leaves the context
+    as it was, and accepts the corrected species afterwards; a Y position
+    one period off is wrapped, as the initial global exchange does."""
+    L = 2 * np.pi
+    rng = np.random.default_rng(2)
+    n = 5000
+    x = rng.uniform(0, L, n)
+    y = rng.uniform(0, L, n)
+    ux = rng.normal(0, 0.1, n)
+    uy = rng.normal(0, 0.1, n)
+    c = _lib.Context(32, 32, L, L, 0.05, precision=prec)
+    for bad in ("x", "ux", "uy", "y"):
+        xs, ys, us, vs = x.copy(), y.copy(), ux.copy(), uy.copy()
+        if bad == "x":
+            xs[17] = L * 1.5
+        elif bad == "ux":
+            us[4000] = np.nan
+        elif bad == "uy":
+            vs[3] = np.inf
+        else:
+            ys[99] = np.nan
+        with pytest.raises(_lib.CpicError) as e:
+            c.add_species(-1.0, 1.0, xs, ys, us, vs)
+        assert e.value.code == -1
+        assert c.lib.cpic_nspecies(c.h) == 0
+    ys = y.copy()
+    ys[5] = y[5] + L                          # one period off in Y
+    c.add_species(-L * L / n, L * L / n, x, ys, ux, uy)
+    c.pre_step()
+    gx, gy, _, _ = c.particles(0)
+    tol = 1e-12 if prec == _lib.FP64 else 1e-6      # mixed: FP32 in-cell offsets
+    assert abs(gy[5] - y[5]) <= tol and c.cell_counts().sum() == n
