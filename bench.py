@@ -259,15 +259,19 @@ def run_ours(args):
         ctx = make_ctx(grid, st, prec, dt)
         ctx.add_species(st["q"], st["m"], host["x"], host["y"], host["ux"], host["uy"])
         ctx.pre_step()
+        ta = time.perf_counter()
         for k in range(e2e_steps):
             ctx.run(1)
             we = ctx.field_energy()
+        tb = time.perf_counter()
         ctx.lib.cpic_get_particles(ctx.h, 0, *[L._dp(a) for a in outx])
         t1 = time.perf_counter()
         ctx.close()
         el = max_over_ranks(t1 - t0)
         out["e2e"] = {"value": ws * n * e2e_steps / el, "unit": UNIT, "steps": e2e_steps,
                       "seconds": el,
+                      "seconds_breakdown": {"create_upload_prestep": ta - t0, "steps": tb - ta,
+                                            "download": t1 - tb},
                       "h2d_bytes_per_step": 4 * 8 * n / e2e_steps,
                       "d2h_bytes_per_step": 4 * 8 * n / e2e_steps + 5 * 8,
                       "host_memory": "pinned" if host["x"].base is not None else "pageable",

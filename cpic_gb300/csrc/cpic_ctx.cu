@@ -532,26 +532,29 @@ static int check_status(cpic_ctx *c)
 
 static int alloc_store(cpic_ctx *c, SpeciesHost &S, int64_t cap, bool alt)
 {
+	// 16 spare records: no bulk copy rounded up to 16 bytes can reach past
+	// the allocation, whatever the last tile's count
+	const int64_t nal = cap + 16;
 	if(c->precision == CPIC_FP64)
 	{
 		StoreF64 &st = alt ? S.f64_alt : S.f64;
-		CK(cudaMalloc(&st.x, cap * sizeof(double)));
-		CK(cudaMalloc(&st.y, cap * sizeof(double)));
-		CK(cudaMalloc(&st.ux, cap * sizeof(double)));
-		CK(cudaMalloc(&st.uy, cap * sizeof(double)));
-		CK(cudaMalloc(&st.id, cap * sizeof(int32_t)));
+		CK(cudaMalloc(&st.x, nal * sizeof(double)));
+		CK(cudaMalloc(&st.y, nal * sizeof(double)));
+		CK(cudaMalloc(&st.ux, nal * sizeof(double)));
+		CK(cudaMalloc(&st.uy, nal * sizeof(double)));
+		CK(cudaMalloc(&st.id, nal * sizeof(int32_t)));
 	}
 	else
 	{
 		StoreMix &st = alt ? S.mix_alt : S.mix;
-		CK(cudaMalloc(&st.cell, cap * sizeof(int32_t)));
-		CK(cudaMalloc(&st.ox, cap * sizeof(float)));
-		CK(cudaMalloc(&st.oy, cap * sizeof(float)));
-		CK(cudaMalloc(&st.ux, cap * sizeof(float)));
-		CK(cudaMalloc(&st.uy, cap * sizeof(float)));
+		CK(cudaMalloc(&st.cell, nal * sizeof(int32_t)));
+		CK(cudaMalloc(&st.ox, nal * sizeof(float)));
+		CK(cudaMalloc(&st.oy, nal * sizeof(float)));
+		CK(cudaMalloc(&st.ux, nal * sizeof(float)));
+		CK(cudaMalloc(&st.uy, nal * sizeof(float)));
 		st.id = nullptr;
 		if(c->p.track_ids)
-			CK(cudaMalloc(&st.id, cap * sizeof(int32_t)));
+			CK(cudaMalloc(&st.id, nal * sizeof(int32_t)));
 	}
 	return CPIC_OK;
 }
@@ -1631,7 +1634,26 @@ struct cpic_ensemble {
 	cudaGraphExec_t exec = nullptr;
 	bool stale = false;       // a run's layout changed since the capture
 	int captures = 0;
+	// what the graph's launches hold by value: every run's current store,
+	// tile layout and spill-list parity at the capture
+	std::vector<const void *> sig;
 };
+
+static std::vector<const void *> ens_sig(const cpic_ensemble *e)
+{
+	std::vector<const void *> v;
+	for(const cpic_ctx *c : e->runs)
+	{
+		v.push_back(reinterpret_cast<const void *>((uintptr_t) c->spill_cur));
+		for(int s = 0; s < c->nspecies; s++)
+		{
+			v.push_back(c->sp[s].f64.x);
+			v.push_back(c->sp[s].mix.cell);
+			v.push_back(c->sp[s].tiles.base);
+		}
+	}
+	return v;
+}
 
 static void ens_drop_graph(cpic_ensemble *e)
 {
@@ -1642,6 +1664,9 @@ static void ens_drop_graph(cpic_ensemble *e)
 static int ens_capture(cpic_ensemble *e)
 {
 	cudaGraph_t graph = nullptr;
+	// two steps swap every spill list twice: the signature after the
+	// capture is the one before it
+	e->sig = ens_sig(e);
 	CK(cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeRelaxed));
 	int r = CPIC_OK;
 	if(cudaEventRecord(e->fork, e->origin) != cudaSuccess) r = CPIC_ECUDA;
@@ -1805,7 +1830,9 @@ CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_gr
 	int64_t pairs = (nsteps - done) / 2;
 	if(pairs > 0)
 	{
-		if((!e->exec || e->stale) && (r = ens_capture(e))) return r;
+		// capture again when a run changed since: a rebuilt layout, or an
+		// odd number of steps taken outside the graph
+		if((!e->exec || e->stale || ens_sig(e) != e->sig) && (r = ens_capture(e))) return r;
 		CK(cudaEventRecord(e->t0, e->origin));
 		float acc = 0.0f;
 		for(int64_t k = 0; k < pairs; k++)

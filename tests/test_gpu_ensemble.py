@@ -49,6 +49,25 @@ def test_ensemble_equals_independent_runs(lib, prec):
     ens.close()
 
 
+def test_ensemble_odd_splits(lib):
+    # calls of 2, 5, 3 and 4 steps: eager single steps between graph
+    # launches flip every run's store and spill parity, so the graph is
+    # captured again whenever it no longer matches
+    runs = [_member(*m, _lib.MIXED) for m in MEMBERS[:3]]
+    ens = _lib.Ensemble(runs)
+    for k in (2, 5, 3, 4):
+        ens.run(k)
+    for m, c in zip(MEMBERS[:3], runs):
+        ref = _member(*m, _lib.MIXED)
+        ref.run(14)
+        assert c.iter == 14
+        for a, b in zip(c.particles(0), ref.particles(0)):
+            assert np.array_equal(a, b)
+        assert c.field_energy() == ref.field_energy()
+        ref.close()
+    ens.close()
+
+
 def _overflowing(prec):
     n = 20000
     rng = np.random.default_rng(3)
