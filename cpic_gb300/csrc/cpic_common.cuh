@@ -36,10 +36,12 @@ constexpr int kPushThreads = CPIC_PUSH_THREADS;
 constexpr int kPPT = CPIC_PPT;                // particles per thread per chunk
 constexpr int kChunk = kPushThreads * kPPT;   // particles per chunk
 constexpr int kWeightBits = 18;
-// folds keep every 32-bit weight sum below 2^31:
-// kFoldChunks * kChunk * 2^kWeightBits <= 2^31
-constexpr int kFoldChunks = (1 << (31 - kWeightBits)) / kChunk;
-static_assert(kFoldChunks >= 1, "chunk too large for 32-bit weight sums");
+// 32-bit shared weight sums: a node gains at most 2^kWeightBits per
+// particle, so kCheckChunks chunks add at most 2^30 to any node; a check
+// every kCheckChunks chunks that finds every node below 2^30 keeps every
+// sum below 2^31 until the next check
+constexpr int kCheckChunks = (1 << (30 - kWeightBits)) / kChunk;
+static_assert(kCheckChunks >= 1, "chunk too large for 32-bit weight sums");
 
 // Device status bits (sticky until the host clears them).
 enum : uint32_t {
@@ -372,6 +374,9 @@ void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		const double *Gt);
 
 void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
+// resident blocks per SM of the mixed fused kernel at this dynamic shared
+// memory (0 on error)
+int push_mix_blocks_per_sm(size_t smem);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
 void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,

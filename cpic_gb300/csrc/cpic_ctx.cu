@@ -507,14 +507,19 @@ static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
 	}
 }
 
-static size_t push_smem(const cpic_ctx *c)
+static size_t push_smem_h(const cpic_ctx *c, int halo)
 {
 	// two staged chunks plus the form's accumulators and field tile
-	int W = c->g.tx + 2 * c->g.halo + 1;
+	int W = c->g.tx + 2 * halo + 1;
 	// (+128: the kernel rounds the dynamic base up to 128 bytes)
 	if(c->precision == CPIC_MIXED)
 		return 128 + 2 * Mix::stage_bytes(c->p.track_ids != 0) + Mix::smem_bytes(W, c->g.tx);
 	return 128 + 2 * F64::stage_bytes(true) + F64::smem_bytes(W, c->g.tx);
+}
+
+static size_t push_smem(const cpic_ctx *c)
+{
+	return push_smem_h(c, c->g.halo);
 }
 
 static int check_status(cpic_ctx *c)
@@ -1185,14 +1190,24 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	r = rebuild_species(c, s, true, &stg, n);
 	free_spill(stg);
 	if(r) return r;
-	// halo: 1.2x the largest initial displacement per step, plus one
-	// (faster particles deposit through global memory: correct, slower)
+	// halo: a particle displaced by at most D cells in a step deposits
+	// into its tile's accumulator when H >= ceil(D).  Take the largest H up
+	// to 1.2 D + 1 (room for the plasma to heat) that keeps as many fused
+	// kernel blocks resident per SM as H = ceil(D) does.  Faster particles
+	// deposit through global memory: correct, slower.
 	vmax = 0.0;
 	for(int k = 0; k < c->nspecies; k++) vmax = std::max(vmax, c->sp[k].vmax);
 	if(c->p.halo <= 0)
 	{
-		int H = (int) ceil(1.2 * vmax * c->p.dt * std::max(c->g.idx, c->g.idy)) + 1;
-		H = std::max(1, std::min(H, c->g.tx));
+		double D = vmax * c->p.dt * std::max(c->g.idx, c->g.idy);
+		int hmin = std::max(1, std::min((int) ceil(D), c->g.tx));
+		int H = std::max(hmin, std::min((int) ceil(1.2 * D) + 1, c->g.tx));
+		if(c->precision == CPIC_MIXED)
+		{
+			int target = push_mix_blocks_per_sm(push_smem_h(c, hmin));
+			while(H > hmin && push_mix_blocks_per_sm(push_smem_h(c, H)) < target)
+				H--;
+		}
 		c->g.halo = H;
 	}
 	return s;

@@ -68,18 +68,56 @@ void launch_gather_mix_tiles(const Grid &g, const StoreMix &st, const int64_t *b
 	k_gather_mix<<<ntiles, 256, 0, s>>>(g, st, base, cnt, E, ex_out, ey_out);
 }
 
+static void push_mix_attrs()
+{
+	static const bool done = [] {
+		const void *fns[2] = {(const void *) k_push<Mix, Mix::kMinBlocks>,
+				(const void *) k_push<Mix, Mix::kHiBlocks>};
+		for(const void *f : fns)
+		{
+			cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+			cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+					cudaSharedmemCarveoutMaxShared);
+		}
+		return true;
+	}();
+	(void) done;
+}
+
+// Whether the register-capped instance of the fused kernel reaches its
+// Mix::kHiBlocks resident blocks per SM with this much dynamic shared
+// memory (else the unconstrained instance runs).
+static bool push_mix_hi(size_t smem)
+{
+	push_mix_attrs();
+	int hi = 0;
+	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, k_push<Mix, Mix::kHiBlocks>,
+			kPushThreads, smem) != cudaSuccess)
+		return false;
+	return hi >= Mix::kHiBlocks;
+}
+
+int push_mix_blocks_per_sm(size_t smem)
+{
+	if(push_mix_hi(smem))
+		return Mix::kHiBlocks;
+	int lo = 0;
+	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, k_push<Mix, Mix::kMinBlocks>,
+			kPushThreads, smem) != cudaSuccess)
+		return 0;
+	return lo;
+}
+
 void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 {
-	static bool init = false;
-	if(!init)
-	{
-		cudaFuncSetAttribute(k_push<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(k_push<Mix>, cudaFuncAttributePreferredSharedMemoryCarveout,
-				cudaSharedmemCarveoutMaxShared);
-		init = true;
-	}
+	const bool hi = push_mix_hi(smem);
 	for(int sp = 0; sp < a.nspecies; sp++)
-		k_push<Mix><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
+	{
+		if(hi)
+			k_push<Mix, Mix::kHiBlocks><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
+		else
+			k_push<Mix, Mix::kMinBlocks><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
+	}
 }
 
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s)

@@ -249,7 +249,9 @@ struct F64 {
 			acc[i] = 0;
 	}
 
-	static __device__ __forceinline__ void fold(unsigned char *, int, int) {}
+	static __device__ __forceinline__ int near_full(unsigned char *, int, int) { return 0; }
+	static __device__ __forceinline__ void fold(const PushArgs &, int, unsigned char *, int, int,
+			int, int) {}
 
 	// Deposit into the tile accumulator, or globally outside the halo, or
 	// with the reference's node indices for the boundary quirk
@@ -346,8 +348,12 @@ struct Mix {
 	struct Rec { int32_t cell; float ox, oy, ux, uy; int32_t id; };
 #ifdef CPIC_PUSH_MIN_BLOCKS
 	static constexpr int kMinBlocks = CPIC_PUSH_MIN_BLOCKS;
+	static constexpr int kHiBlocks = CPIC_PUSH_MIN_BLOCKS;
 #else
 	static constexpr int kMinBlocks = kPushThreads >= 1024 ? 1 : 1024 / kPushThreads;
+	// second instance, registers capped for 48 resident warps per SM: used
+	// when that many blocks fit in shared memory
+	static constexpr int kHiBlocks = kPushThreads >= 1536 ? 1 : 1536 / kPushThreads;
 #endif
 
 	struct Out {
@@ -357,12 +363,11 @@ struct Mix {
 		uint32_t err;
 	};
 
-	// shared memory: W x W u32 accumulator, W x W u64 shadow, then the
-	// (T+1) x (T+1) E tile
+	// shared memory: the (T+1) x (T+1) E tile, then the W x W u32
+	// accumulator
 	static __host__ __device__ size_t smem_bytes(int W, int T)
 	{
-		return (size_t) W * W * (sizeof(uint32_t) + sizeof(unsigned long long))
-			+ (size_t) (T + 1) * (T + 1) * sizeof(float2);
+		return (size_t) W * W * sizeof(uint32_t) + (size_t) (T + 1) * (T + 1) * sizeof(float2);
 	}
 
 	static __device__ __forceinline__ Rec load(const PushArgs &a, int s, int64_t i)
@@ -519,42 +524,51 @@ struct Mix {
 		return o;
 	}
 
-	// Shared layout, every array on its natural alignment (W is odd, so
-	// the 8-byte arrays come first): [u64 shadow W*W][float2 E tile
-	// (T+1)^2][u32 accumulator W*W].
-	static __device__ __forceinline__ unsigned long long *sh64(unsigned char *sm)
+	// Shared layout: [float2 E tile (T+1)^2][u32 accumulator W*W].
+	static __device__ __forceinline__ float2 *shE(unsigned char *sm, int)
 	{
-		return reinterpret_cast<unsigned long long *>(sm);
+		return reinterpret_cast<float2 *>(sm);
 	}
-	static __device__ __forceinline__ float2 *shE(unsigned char *sm, int W)
+	static __device__ __forceinline__ uint32_t *sh32(unsigned char *sm, int, int T)
 	{
-		return reinterpret_cast<float2 *>(sm + (size_t) W * W * 8);
-	}
-	static __device__ __forceinline__ uint32_t *sh32(unsigned char *sm, int W, int T)
-	{
-		return reinterpret_cast<uint32_t *>(sm + (size_t) W * W * 8 + (size_t) (T + 1) * (T + 1) * 8);
+		return reinterpret_cast<uint32_t *>(sm + (size_t) (T + 1) * (T + 1) * 8);
 	}
 
 	static __device__ __forceinline__ void clear(unsigned char *sm, int W, int T)
 	{
 		uint32_t *a32 = sh32(sm, W, T);
-		unsigned long long *a64 = sh64(sm);
 		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
-		{
 			a32[i] = 0;
-			a64[i] = 0;
-		}
 	}
 
-	// Move the 32-bit sums into the 64-bit shadow (between barriers).
-	static __device__ __forceinline__ void fold(unsigned char *sm, int W, int T)
+	// Some node's sum has reached 2^30 (this thread's share of the nodes).
+	static __device__ __forceinline__ int near_full(unsigned char *sm, int W, int T)
 	{
-		uint32_t *a32 = sh32(sm, W, T);
-		unsigned long long *a64 = sh64(sm);
+		const uint32_t *a32 = sh32(sm, W, T);
+		uint32_t m = 0;
+		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
+			m |= a32[i];
+		return (m >> 30) != 0;
+	}
+
+	// Add the 32-bit sums to global rho and restart them from zero
+	// (between barriers).  With the species' fixed-point factor an exact
+	// integer, the partial sums add up to exactly the value one flush of
+	// the whole tile gives.
+	static __device__ __forceinline__ void fold(const PushArgs &a, int s, unsigned char *sm,
+			int W, int H, int tx0, int ty0)
+	{
+		uint32_t *a32 = sh32(sm, W, a.g.tx);
+		double sc = a.sp[s].wq_scale;
 		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
 		{
-			a64[i] += a32[i];
-			a32[i] = 0;
+			uint32_t v = a32[i];
+			if(v != 0)
+			{
+				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)],
+						__double2ll_rn((double) v * sc));
+				a32[i] = 0;
+			}
 		}
 	}
 
@@ -583,11 +597,10 @@ struct Mix {
 			int W, int H, int tx0, int ty0)
 	{
 		const uint32_t *a32 = sh32(sm, W, a.g.tx);
-		const unsigned long long *a64 = sh64(sm);
 		double sc = a.sp[s].wq_scale;
 		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
 		{
-			unsigned long long v = a64[i] + a32[i];
+			uint32_t v = a32[i];
 			if(v != 0)
 				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)],
 						__double2ll_rn((double) v * sc));
@@ -656,8 +669,8 @@ struct Mix {
 
 // ============================================================== kernels
 
-template <class F>
-__global__ void __launch_bounds__(kPushThreads, F::kMinBlocks)
+template <class F, int MinBlocks = F::kMinBlocks>
+__global__ void __launch_bounds__(kPushThreads, MinBlocks)
 k_push(const PushArgs a)
 {
 	// dynamic shared memory: two staged chunks, then the form's area
@@ -722,13 +735,17 @@ k_push(const PushArgs a)
 	for(int ci = 0; ci < nchunks; ci++)
 	{
 		const int c0 = ci * kChunk;
-		if(ci > 0 && ci % kFoldChunks == 0)
+		if(ci > 0 && ci % kCheckChunks == 0)
 		{
-			// every deposit of the previous chunks precedes the fold, and
-			// the fold precedes every later deposit
-			__syncthreads();
-			F::fold(fsm, W, g.tx);
-			__syncthreads();
+			// every deposit of the previous chunks precedes the check (and
+			// the fold), and the fold precedes every later deposit.  At
+			// typical densities a node's sum over the whole tile stays far
+			// below 2^30 and the fold never runs.
+			if(__syncthreads_or(F::near_full(fsm, W, g.tx)))
+			{
+				F::fold(a, s, fsm, W, H, tx0, ty0);
+				__syncthreads();
+			}
 		}
 		// prefetch the next chunk into the other buffer once every warp
 		// has released it (its last reader was chunk ci - 1)

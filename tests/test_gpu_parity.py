@@ -279,6 +279,29 @@ def test_mixed_form_independent_of_rebuild_schedule(lib):
     assert a.field_energy() == b.field_energy()
 
 
+def test_mixed_deposit_pileup(lib):
+    """Mixed form: 300,000 particles in one cell.  Each of its nodes gathers
+    about 2^34 weight quanta, far past the 32-bit shared sums, so the fused
+    kernel must move them to global rho whenever one nears 2^31; rho then
+    agrees with the oracle's within the weight quantisation."""
+    n = 300000
+    L = 2 * np.pi
+    rng = np.random.default_rng(21)
+    h = L / 64
+    x = (10 + rng.uniform(0, 1, n)) * h
+    y = (37 + rng.uniform(0, 1, n)) * h
+    z = np.zeros(n)
+    q = -L * L / n
+    case = dict(nx=64, ny=64, L=L, dt=0.05, B=(0.0, 0.0, 0.0), steps=1,
+                species=[dict(q=q, m=-q, x=x, y=y, ux=z, uy=z)])
+    g = cases.make_gpu(case, precision=_lib.MIXED, tile=8, halo=1)
+    o = cases.make_oracle(case)
+    g.pre_step()
+    o.pre_step()
+    assert rel_max(g.rho(), o.rho()) <= 1e-5
+    assert abs(g.rho().sum() - o.rho().sum()) <= 1e-5 * abs(o.rho().sum())
+
+
 @pytest.mark.parametrize("prec", [_lib.FP64, _lib.MIXED], ids=["fp64", "mixed"])
 def test_invalid_uploads_are_rejected(lib, prec):
     """cpic_add_species refuses positions outside [0, Lx] in X and
