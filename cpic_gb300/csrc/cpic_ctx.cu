@@ -168,13 +168,33 @@ __global__ void k_rb_scatter(const PushArgs newa, int s, Spill S, int64_t n, int
 	}
 }
 
-// Upload counting sort with block-local histograms (shared-memory atomics,
-// one global atomic per block and bin): the bins are (tile, sign of ux), so
-// inside every tile the particles moving left come first and those moving
-// right after them.  Warps then mostly hold particles leaving towards the
-// same neighbour from the first step on, as the in-place re-bin makes them
-// after a tile's population has been renewed.  Blocks take contiguous
-// ranges.  Shared memory: 2 nt (count) or 4 nt (scatter) ints.
+// Tile of a record in the store layout.
+template <class F> struct RecTile;
+template <> struct RecTile<F64> {
+	static __device__ __forceinline__ int get(const Grid &g, const F64::Rec &r)
+	{
+		double w[4];
+		int cx, cy;
+		F64::weights(g, r.x, r.y, w, cx, cy);
+		cx = min(max(cx, 0), g.nx - 1);
+		cy = min(max(cy, 0), g.ny - 1);
+		return tile_of(g, cx, cy);
+	}
+};
+template <> struct RecTile<Mix> {
+	static __device__ __forceinline__ int get(const Grid &g, const Mix::Rec &r)
+	{
+		return tile_of(g, r.cell & (g.nx - 1), r.cell >> g.lnx);
+	}
+};
+
+// Upload counting sort, histogram: block-local counts (shared-memory
+// atomics, one global atomic per block and bin) of the bins (tile, sign of
+// ux).  The sort (k_rb_pass) places inside every tile the particles moving
+// left first and those moving right after them: warps then mostly hold
+// particles leaving towards the same neighbour from the first step on, as
+// the in-place re-bin makes them after a tile's population has been
+// renewed.  Blocks take contiguous ranges.  Shared memory: 2 nt ints.
 template <class F>
 __global__ void k_rb_count_blk(Grid g, Spill S, int64_t n, int nt, int32_t *cnt, int32_t *neg)
 {
@@ -185,8 +205,9 @@ __global__ void k_rb_count_blk(Grid g, Spill S, int64_t n, int nt, int32_t *cnt,
 	int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
 	for(int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
 	{
-		int t = TileOf<F>::get(g, S, k);
-		atomicAdd(&shb[(S.ux[k] >= 0.0 ? nt : 0) + t], 1);
+		// the record as the sort sees it (the same tile and sign test)
+		typename F::Rec r = F::from_spill(S, k, g);
+		atomicAdd(&shb[(r.ux >= 0 ? nt : 0) + RecTile<F>::get(g, r)], 1);
 	}
 	__syncthreads();
 	for(int t = threadIdx.x; t < nt; t += blockDim.x)
@@ -197,39 +218,81 @@ __global__ void k_rb_count_blk(Grid g, Spill S, int64_t n, int nt, int32_t *cnt,
 	}
 }
 
-template <class F>
-__global__ void k_rb_scatter_blk(const PushArgs na, int s, Spill S, int64_t n, int nt,
-		int32_t *fneg, int32_t *fpos)
+// One pass of the upload sort.  Blocks take contiguous ranges of the input
+// and move it in batches of kRbPer x blockDim records: a shared histogram
+// ranks each record within its bucket, the first record of every bucket
+// reserves the batch's run at the bucket's cursor with one 64-bit global
+// atomic, and the records are written to their runs.  Every run is
+// contiguous and written within one batch, so its cache lines are whole
+// before they leave L2.  Pass 1 (from the FP64 staging list): buckets are
+// rows of tiles, output a temporary store grouped by row.  Pass 2 (from
+// that store): buckets are (direction of ux, tile), so inside every tile
+// the particles moving left come first; output the new layout.  Shared
+// memory: nb 64-bit offsets, then nb counters.
+constexpr int kRbPer = 4;
+constexpr int kRbThreads = 512;
+
+template <class F, bool kFromStaging>
+__global__ void __launch_bounds__(kRbThreads)
+k_rb_pass(const PushArgs in, const PushArgs out, int s, Spill S, int64_t n, int nb,
+		unsigned long long *cursor)
 {
-	extern __shared__ int32_t shb[];
-	int32_t *bb = shb + 2 * nt;
-	const Grid &g = na.g;
-	for(int i = threadIdx.x; i < 2 * nt; i += blockDim.x) shb[i] = 0;
+	extern __shared__ __align__(8) unsigned char shraw[];
+	unsigned long long *off = reinterpret_cast<unsigned long long *>(shraw);
+	int32_t *hist = reinterpret_cast<int32_t *>(shraw + (size_t) nb * 8);
+	const Grid &g = out.g;
+	const int nt = g.ntx * g.nty;
+	for(int i = threadIdx.x; i < nb; i += blockDim.x) hist[i] = 0;
 	__syncthreads();
-	int64_t per = (n + gridDim.x - 1) / gridDim.x;
-	int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
-	for(int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
+	const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+	const int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
+	for(int64_t b0 = lo; b0 < hi; b0 += (int64_t) kRbPer * blockDim.x)
 	{
-		int t = TileOf<F>::get(g, S, k);
-		atomicAdd(&shb[(S.ux[k] >= 0.0 ? nt : 0) + t], 1);
+		typename F::Rec r[kRbPer];
+		int key[kRbPer], rank[kRbPer];
+		#pragma unroll
+		for(int k = 0; k < kRbPer; k++)
+		{
+			const int64_t i = b0 + (int64_t) k * blockDim.x + threadIdx.x;
+			key[k] = -1;
+			rank[k] = 0;
+			if(i < hi)
+			{
+				if(kFromStaging)
+					r[k] = F::from_spill(S, i, g);
+				else
+					r[k] = F::load(in, s, i);
+				const int t = RecTile<F>::get(g, r[k]);
+				key[k] = kFromStaging ? t >> (g.lnx - g.ltx) : (r[k].ux >= 0 ? nt : 0) + t;
+				rank[k] = atomicAdd(&hist[key[k]], 1);
+			}
+		}
+		__syncthreads();
+		#pragma unroll
+		for(int k = 0; k < kRbPer; k++)
+			if(key[k] >= 0 && rank[k] == 0)
+				off[key[k]] = atomicAdd(&cursor[key[k]], (unsigned long long) hist[key[k]]);
+		__syncthreads();
+		#pragma unroll
+		for(int k = 0; k < kRbPer; k++)
+			if(key[k] >= 0)
+			{
+				F::store(out, s, (int64_t) off[key[k]] + rank[k], r[k]);
+				hist[key[k]] = 0;
+			}
+		__syncthreads();
 	}
-	__syncthreads();
-	for(int t = threadIdx.x; t < nt; t += blockDim.x)
+}
+
+// Pass-2 cursors: left movers of tile t from base[t], right movers after
+// all of them.
+__global__ void k_rb_cursors(int nt, const int64_t *base, const int32_t *neg,
+		unsigned long long *cur)
+{
+	for(int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x)
 	{
-		int a = shb[t], b = shb[nt + t];
-		bb[t] = a ? atomicAdd(&fneg[t], a) : 0;
-		bb[nt + t] = b ? atomicAdd(&fpos[t], b) : 0;
-		shb[t] = 0;
-		shb[nt + t] = 0;
-	}
-	__syncthreads();
-	for(int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
-	{
-		int t = TileOf<F>::get(g, S, k);
-		int j = (S.ux[k] >= 0.0 ? nt : 0) + t;
-		int slot = bb[j] + atomicAdd(&shb[j], 1);
-		typename F::Rec r = F::from_spill(S, k, g);
-		F::store(na, s, na.tiles[s].base[t] + slot, r);
+		cur[t] = (unsigned long long) base[t];
+		cur[nt + t] = (unsigned long long) (base[t] + neg[t]);
 	}
 }
 
@@ -661,8 +724,6 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 			const int mx = 4 * kBlkSortMaxTiles * (int) sizeof(int32_t);
 			cudaFuncSetAttribute(k_rb_count_blk<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 			cudaFuncSetAttribute(k_rb_count_blk<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			cudaFuncSetAttribute(k_rb_scatter_blk<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			cudaFuncSetAttribute(k_rb_scatter_blk<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 			attr = true;
 		}
 		CK(cudaMalloc(&negcnt, nt * sizeof(int32_t)));
@@ -738,19 +799,54 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	}
 	if(blk)
 	{
-		// left movers from slot 0, right movers after all of them
-		int32_t *fpos = nullptr;
-		CK(cudaMalloc(&fpos, nt * sizeof(int32_t)));
-		CK(cudaMemcpyAsync(fpos, negcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
-		size_t sm = 4 * (size_t) nt * sizeof(int32_t);
+		// pass 1: by row of tiles into a temporary store; pass 2: by
+		// (direction, tile) into the new layout
+		const int ltxn = c->g.lnx - c->g.ltx;          // log2 tiles per row
+		const int nrow = nt >> ltxn;
+		std::vector<unsigned long long> rowcur(nrow);
+		unsigned long long acc = 0;
+		for(int r = 0; r < nrow; r++)
+		{
+			rowcur[r] = acc;
+			for(int t = r << ltxn; t < (r + 1) << ltxn; t++) acc += (unsigned long long) hc[t];
+		}
+		SpeciesHost tmp;
+		memset(&tmp, 0, sizeof(tmp));
+		int r = alloc_store(c, tmp, nstage, false);
+		if(r) return r;
+		PushArgs tmpa = newa;
+		tmpa.f64[s] = tmp.f64;
+		tmpa.mix[s] = tmp.mix;
+		unsigned long long *cur = nullptr;
+		CK(cudaMalloc(&cur, std::max(nrow, 2 * nt) * sizeof(unsigned long long)));
+		CK(cudaMemcpyAsync(cur, rowcur.data(), nrow * sizeof(unsigned long long),
+				cudaMemcpyHostToDevice, st));
+		static bool pattr = false;
+		if(!pattr)
+		{
+			const int mx = 2 * kBlkSortMaxTiles * 12;
+			cudaFuncSetAttribute(k_rb_pass<Mix, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			cudaFuncSetAttribute(k_rb_pass<F64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			cudaFuncSetAttribute(k_rb_pass<Mix, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			cudaFuncSetAttribute(k_rb_pass<F64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			pattr = true;
+		}
+		const int pb = 152 * 2;
+		size_t sm1 = (size_t) nrow * 12, sm2 = (size_t) 2 * nt * 12;
 		if(mix)
-			k_rb_scatter_blk<Mix><<<blk_blocks, 512, sm, st>>>(newa, s, *staging, nstage, nt, fill,
-					fpos);
+			k_rb_pass<Mix, true><<<pb, kRbThreads, sm1, st>>>(tmpa, tmpa, s, *staging, nstage, nrow, cur);
 		else
-			k_rb_scatter_blk<F64><<<blk_blocks, 512, sm, st>>>(newa, s, *staging, nstage, nt, fill,
-					fpos);
+			k_rb_pass<F64, true><<<pb, kRbThreads, sm1, st>>>(tmpa, tmpa, s, *staging, nstage, nrow, cur);
+		CK(cudaGetLastError());
+		k_rb_cursors<<<(nt + 255) / 256, 256, 0, st>>>(nt, nbase, negcnt, cur);
+		if(mix)
+			k_rb_pass<Mix, false><<<pb, kRbThreads, sm2, st>>>(tmpa, newa, s, *staging, nstage, 2 * nt, cur);
+		else
+			k_rb_pass<F64, false><<<pb, kRbThreads, sm2, st>>>(tmpa, newa, s, *staging, nstage, 2 * nt, cur);
+		CK(cudaGetLastError());
 		CK(cudaStreamSynchronize(st));
-		cudaFree(fpos);
+		cudaFree(cur);
+		free_store(c, tmp, false);
 		cudaFree(negcnt);
 	}
 	else if(mix)
