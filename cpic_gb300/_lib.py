@@ -283,7 +283,7 @@ class Context:
     def layout_stats(self):
         out = (ctypes.c_int64 * 4)()
         self._check(self.lib.cpic_layout_stats(self.h, out), "cpic_layout_stats")
-        return dict(last_spill=out[0], rebuilds=out[1], slack_pct=out[2])
+        return dict(last_spill=out[0], rebuilds=out[1], slack_pct=out[2], blocks_per_sm=out[3])
 
     def tile_info(self):
         out = (ctypes.c_int32 * 4)()

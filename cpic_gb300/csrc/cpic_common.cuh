@@ -366,6 +366,7 @@ spill_push(const Spill &S, double x, double y, double ux, double uy, int32_t id)
 // Launchers implemented in the per-precision translation units.
 namespace cpic {
 void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
+int push_f64_blocks_per_sm(size_t smem);
 void launch_spill_f64(const SpillArgs &a, cudaStream_t s);
 void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s);
 void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,

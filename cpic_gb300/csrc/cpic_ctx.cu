@@ -1687,6 +1687,13 @@ CPIC_API int cpic_layout_stats(const cpic_ctx_t *c, int64_t *out)
 	out[1] = c->rebuilds;
 	out[2] = c->slack_pct;
 	out[3] = 0;
+	if(c->nspecies > 0)
+	{
+		if(c->precision == CPIC_MIXED)
+			out[3] = push_mix_blocks_per_sm(push_smem(c));
+		else
+			out[3] = push_f64_blocks_per_sm(push_smem(c));
+	}
 	return CPIC_OK;
 }
 

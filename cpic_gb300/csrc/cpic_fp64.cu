@@ -67,16 +67,30 @@ void launch_gather_f64_tiles(const Grid &g, const StoreF64 &st, const int64_t *b
 	k_gather_f64<<<ntiles, 256, 0, s>>>(g, st, base, cnt, Ex, Ey, ex_out, ey_out);
 }
 
-void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+static void push_f64_attrs()
 {
-	static bool init = false;
-	if(!init)
-	{
+	static const bool done = [] {
 		cudaFuncSetAttribute(k_push<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 		cudaFuncSetAttribute(k_push<F64>, cudaFuncAttributePreferredSharedMemoryCarveout,
 				cudaSharedmemCarveoutMaxShared);
-		init = true;
-	}
+		return true;
+	}();
+	(void) done;
+}
+
+int push_f64_blocks_per_sm(size_t smem)
+{
+	push_f64_attrs();
+	int b = 0;
+	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_push<F64>, kPushThreads, smem)
+			!= cudaSuccess)
+		return 0;
+	return b;
+}
+
+void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+{
+	push_f64_attrs();
 	for(int sp = 0; sp < a.nspecies; sp++)
 		k_push<F64><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
 }

@@ -178,7 +178,8 @@ CPIC_API int cpic_tile_info(const cpic_ctx_t *ctx, int32_t *out);
 /* Health of the tile layout, out[4]: {overflow records (particles that
  * found no room in their destination tile) seen at the last host check,
  * layout rebuilds forced by overflows so far, current capacity slack in
- * percent, 0}. */
+ * percent, resident blocks per SM of the fused particle kernel at this
+ * context's tile and halo (0 before the first species)}. */
 CPIC_API int cpic_layout_stats(const cpic_ctx_t *ctx, int64_t *out);
 
 /* --- solve without allocation ------------------------------------------ */
