@@ -382,5 +382,5 @@ void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
 void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
-		const double *cosy, float *phi, cudaStream_t s, const float *Gt);
+		const double *cosy, float *phi, cudaStream_t s, const float *Gt, double mean0 = 0.0);
 } // namespace cpic

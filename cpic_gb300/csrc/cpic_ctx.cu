@@ -77,7 +77,6 @@ struct cpic_ctx {
 	double *green64;          // Green's function, column order (FP64 form)
 	float *green32;           // same, FP32 (mixed form)
 	double *mean;             // device scalar (mixed form)
-	long long *rho_sum;       // device scalar
 	uint32_t *status;
 	double *scratch;          // FP64 scratch for host views / partial sums
 	size_t scratch_n;
@@ -437,26 +436,6 @@ __global__ void k_field_energy(Grid g, const double *Ex, const double *Ey, const
 		part[2 * iy] = sh[0][0];
 		part[2 * iy + 1] = (double) shq[0];
 	}
-}
-
-// Exact int64 sum of rho (the k = 0 mode of the mixed form, removed in FP64
-// before the FP32 transform).  Integer adds: any order gives the same sum.
-__global__ void k_rho_sum(int64_t n, const long long *rho, long long *sum)
-{
-	__shared__ long long sh[256];
-	long long v = 0;
-	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
-			i += (int64_t) gridDim.x * blockDim.x)
-		v += rho[i];
-	sh[threadIdx.x] = v;
-	__syncthreads();
-	for(int st = blockDim.x / 2; st > 0; st >>= 1)
-	{
-		if(threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
-		__syncthreads();
-	}
-	if(threadIdx.x == 0)
-		atomicAdd((unsigned long long *) sum, (unsigned long long) sh[0]);
 }
 
 // Fixed point -> FP64; rlo (FP64 form) adds the remainder word.
@@ -957,11 +936,15 @@ static int field_stage_async(cpic_ctx *c)
 	cudaStream_t st = c->stream;
 	if(c->precision == CPIC_MIXED)
 	{
-		int64_t ng = (int64_t) c->g.nx * c->g.ny;
-		CK(cudaMemsetAsync(c->rho_sum, 0, sizeof(long long), st));
-		k_rho_sum<<<grid_blocks(ng, 256, 2 * 152), 256, 0, st>>>(ng, c->rho, c->rho_sum);
-		launch_poisson_mix(c->g, c->rho, c->qinv, c->rho_sum, c->spec32, c->twx32, c->twy32,
-				c->cosx, c->cosy, c->phi32, st, c->green32);
+		// the mean charge density the particles carry (each deposits
+		// -q/e0 in all, sum_s n_s (-q_s/e0) over the nx ny nodes): removed
+		// before the FP32 transform
+		double tot = 0.0;
+		for(int s = 0; s < c->nspecies; s++)
+			tot += (double) c->sp[s].n * (-c->sp[s].q / c->p.e0);
+		double mean0 = tot / ((double) c->g.nx * (double) c->g.ny);
+		launch_poisson_mix(c->g, c->rho, c->qinv, nullptr, c->spec32, c->twx32, c->twy32,
+				c->cosx, c->cosy, c->phi32, st, c->green32, mean0);
 		launch_E_mix(c->g, c->phi32, c->E32, st);
 	}
 	else
@@ -1062,7 +1045,6 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	AL(c->cosx, g.nx * sizeof(double));
 	AL(c->cosy, g.ny * sizeof(double));
 	AL(c->mean, sizeof(double));
-	AL(c->rho_sum, sizeof(long long));
 	AL(c->counter, sizeof(int32_t));
 	AL(c->counter_pair, 2 * sizeof(unsigned long long));
 	if(c->precision == CPIC_FP64)
@@ -1162,7 +1144,7 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 	cudaFree(c->rho); cudaFree(c->rho_lo); cudaFree(c->phi64); cudaFree(c->Ex64); cudaFree(c->Ey64);
 	cudaFree(c->phi32); cudaFree(c->E32); cudaFree(c->spec64); cudaFree(c->spec32);
 	cudaFree(c->twx64); cudaFree(c->twy64); cudaFree(c->twx32); cudaFree(c->twy32);
-	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->green64); cudaFree(c->green32); cudaFree(c->mean); cudaFree(c->rho_sum);
+	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->green64); cudaFree(c->green32); cudaFree(c->mean);
 	cudaFree(c->status); cudaFree(c->scratch); cudaFree(c->counter); cudaFree(c->counter_pair);
 	if(c->stream) cudaStreamDestroy(c->stream);
 	delete c;

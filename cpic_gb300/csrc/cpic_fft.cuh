@@ -5,7 +5,7 @@
 // Replaces MFT_solve (src/solver.c:465-509): phi = IFFT(G * FFT(rho)) / (nx
 // ny) with G(kx,ky) = 1 / (2 (cos(2 pi kx/nx) + cos(2 pi ky/ny)) - 4) and
 // G(0,0) = 0 (solver.c:269-280).  Three kernels, all working in shared
-// memory with Stockham radix-2 passes (self-sorting, no bit reversal):
+// memory with Stockham radix-4 passes (self-sorting, no bit reversal):
 //   rows_fwd : two real rows packed as one complex row, FFT along x, split
 //              into the two half spectra (nx/2+1 bins each);
 //   cols     : a block of spectrum columns, FFT along y, multiply by G,
@@ -37,34 +37,77 @@ __device__ __forceinline__ C cmul(C a, C b)
 	return r;
 }
 
+// Twiddle exp(-2 pi i m / n) for 0 <= m < n from the half table
+// tw[m] (m < n/2): exp(-2 pi i (m + n/2) / n) = -exp(-2 pi i m / n).
+template <typename C>
+__device__ __forceinline__ C twiddle(const C *tw, int m, int half, int sign)
+{
+	C w = m < half ? tw[m] : tw[m - half];
+	if(m >= half) { w.x = -w.x; w.y = -w.y; }
+	if(sign > 0) w.y = -w.y;
+	return w;
+}
+
 // nb independent length-n sequences stored back to back in `a`; `b` is
 // scratch of the same size.  tw[k] = exp(-2 pi i k / n), k < n/2.  sign
 // -1 forward, +1 inverse (unnormalised).  Returns the buffer holding the
 // result.  Must be called by the whole block.
+//
+// Stockham autosort passes (no bit reversal): one radix-2 pass first when
+// log2 n is odd (sub-transforms of length 1: unit twiddles), then radix-4
+// passes.  A radix-4 pass with sub-transform length Ns takes x[j + q n/4],
+// q = 0..3, twiddles them by exp(sign 2 pi i q k / (4 Ns)) (k = j mod Ns)
+// and writes their 4-point DFT to y[4 (j - k) + k + p Ns], p = 0..3: half
+// as many passes and block barriers as radix 2.
 template <typename C>
 __device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *tw)
 {
-	int half = n >> 1;
-	int total = half * nb;
-	for(int s = 0; s < log2n; s++)
+	const int half = n >> 1;
+	int Ns = 1, s = 0;
+	if(log2n & 1)
 	{
-		int Ns = 1 << s;
-		int tshift = log2n - 1 - s;     // n / (2 Ns) = 2^tshift
+		const int total = half * nb;
 		for(int idx = threadIdx.x; idx < total; idx += blockDim.x)
 		{
 			int seq = idx >> (log2n - 1);
 			int j = idx & (half - 1);
-			C *x = a + seq * n;
+			const C *x = a + seq * n;
+			C *y = b + seq * n;
+			C a0 = x[j], a1 = x[j + half];
+			y[2 * j] = cadd(a0, a1);
+			y[2 * j + 1] = csub(a0, a1);
+		}
+		__syncthreads();
+		C *t = a; a = b; b = t;
+		Ns = 2;
+		s = 1;
+	}
+	const int q4 = n >> 2;
+	for(; Ns < n; Ns <<= 2, s += 2)
+	{
+		const int total = q4 * nb;
+		const int sh = log2n - 2 - s;        // n / (4 Ns) = 2^sh
+		for(int idx = threadIdx.x; idx < total; idx += blockDim.x)
+		{
+			int seq = idx >> (log2n - 2);
+			int j = idx & (q4 - 1);
+			const C *x = a + seq * n;
 			C *y = b + seq * n;
 			int k = j & (Ns - 1);
-			C a0 = x[j];
-			C a1 = x[j + half];
-			C w = tw[k << tshift];
-			if(sign > 0) w.y = -w.y;
-			a1 = cmul(a1, w);
-			int o = ((j - k) << 1) + k;
-			y[o] = cadd(a0, a1);
-			y[o + Ns] = csub(a0, a1);
+			C v0 = x[j];
+			C v1 = cmul(x[j + q4], twiddle(tw, k << sh, half, sign));
+			C v2 = cmul(x[j + 2 * q4], twiddle(tw, (2 * k) << sh, half, sign));
+			C v3 = cmul(x[j + 3 * q4], twiddle(tw, (3 * k) << sh, half, sign));
+			C t0 = cadd(v0, v2), t1 = csub(v0, v2), t2 = cadd(v1, v3), t3 = csub(v1, v3);
+			// t3 times -i (forward) or +i (inverse)
+			C r3;
+			if(sign < 0) { r3.x = t3.y; r3.y = -t3.x; }
+			else { r3.x = -t3.y; r3.y = t3.x; }
+			int o = ((j - k) << 2) + k;
+			y[o] = cadd(t0, t2);
+			y[o + Ns] = cadd(t1, r3);
+			y[o + 2 * Ns] = csub(t0, t2);
+			y[o + 3 * Ns] = csub(t1, r3);
 		}
 		__syncthreads();
 		C *t = a; a = b; b = t;
@@ -74,14 +117,18 @@ __device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *
 
 // rho (fixed point, ny x nx) -> spec (ny x (nx/2+1)).  One block per row
 // pair.  value = (double) acc * qinv - mean, where the mean (the k = 0
-// mode, removed in FP64 before the FP32 transform of the mixed form) comes
-// from the exact integer sum rsum; rsum null: no removal (FP64 form, as the
-// reference, whose G(0,0) = 0 discards the mode).
+// mode, removed in FP64 before the FP32 transform of the mixed form, so
+// that the transform's rounding scales with the fluctuations, not with the
+// total charge) comes from the exact integer sum rsum, or is mean0 when
+// rsum is null.  G(0,0) = 0 discards whatever is left of the mode, so mean0
+// may be the charge the particles carry (the deposit's weight rounding
+// leaves a residue of ~2^-17 of it).  FP64 form: no removal (as the
+// reference).
 // rho_lo (FP64 form, may be null): the remainder word at scale qinv_lo.
 template <typename T>
 __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, double qinv,
 		const long long *rsum, typename Cx<T>::t *spec, const typename Cx<T>::t *tw,
-		const long long *rho_lo, double qinv_lo)
+		const long long *rho_lo, double qinv_lo, double mean0)
 {
 	typedef typename Cx<T>::t C;
 	extern __shared__ unsigned char smem_raw[];
@@ -89,7 +136,7 @@ __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, dou
 	C *b = a + nx;
 	int r0 = 2 * blockIdx.x;
 	int nh = nx / 2 + 1;
-	double m = rsum ? (double) *rsum * qinv / ((double) nx * (double) ny) : 0.0;
+	double m = rsum ? (double) *rsum * qinv / ((double) nx * (double) ny) : mean0;
 	for(int i = threadIdx.x; i < nx; i += blockDim.x)
 	{
 		int64_t ia = (int64_t) r0 * nx + i, ib = (int64_t) (r0 + 1) * nx + i;
@@ -155,9 +202,13 @@ __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *sp
 	int ncol = min(cb, nh - c0);
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + (size_t) cb * ny;
+	// element idx of the block's columns: row idx / ncol, column idx % ncol
+	// (a shift and a mask when ncol is a power of two, as it is except
+	// for small grids)
+	const int lg = (ncol & (ncol - 1)) == 0 ? __ffs(ncol) - 1 : -1;
 	for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
 	{
-		int row = idx / ncol, c = idx - row * ncol;
+		int row = lg >= 0 ? idx >> lg : idx / ncol, c = idx - row * ncol;
 		a[c * ny + row] = spec[(int64_t) row * nh + c0 + c];
 	}
 	__syncthreads();
@@ -178,7 +229,7 @@ __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *sp
 	{
 		for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
 		{
-			int c = idx / ny, row = idx - c * ny;
+			int c = idx >> log2ny, row = idx - (c << log2ny);
 			int kx = c0 + c;
 			double G = (kx == 0 && row == 0) ? 0.0 : 1.0 / (2.0 * (cosx[kx] + cosy[row]) - 4.0);
 			C v = X[idx];
@@ -192,7 +243,7 @@ __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *sp
 	C *R = fft_smem<C>(X, Y, ny, log2ny, ncol, +1, tw);
 	for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
 	{
-		int row = idx / ncol, c = idx - row * ncol;
+		int row = lg >= 0 ? idx >> lg : idx / ncol, c = idx - row * ncol;
 		spec[(int64_t) row * nh + c0 + c] = R[c * ny + row];
 	}
 }
@@ -278,7 +329,8 @@ template <typename T>
 static void poisson_launch(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		typename Cx<T>::t *spec, const typename Cx<T>::t *twx, const typename Cx<T>::t *twy,
 		const double *cosx, const double *cosy, T *phi, cudaStream_t s,
-		const long long *rho_lo = nullptr, double qinv_lo = 0.0, const T *Gt = nullptr)
+		const long long *rho_lo = nullptr, double qinv_lo = 0.0, const T *Gt = nullptr,
+		double mean0 = 0.0)
 {
 	typedef typename Cx<T>::t C;
 	int log2nx = 0, log2ny = 0;
@@ -287,7 +339,7 @@ static void poisson_launch(const Grid &g, const long long *rho, double qinv, con
 	int rthreads = g.nx / 2 < 512 ? (g.nx / 2 < 32 ? 32 : g.nx / 2) : 512;
 	size_t rsm = 2 * (size_t) g.nx * sizeof(C);
 	k_rows_fwd<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, rho, qinv, mean, spec, twx,
-			rho_lo, qinv_lo);
+			rho_lo, qinv_lo, mean0);
 	int nh = g.nx / 2 + 1;
 	// columns per block: up to 64 KB of shared memory (two buffers), so
 	// that several blocks share an SM

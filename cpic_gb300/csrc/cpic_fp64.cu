@@ -17,12 +17,13 @@ __global__ void k_E_f64(Grid g, const double *phi, double *Ex, double *Ey)
 	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
 			i += (int64_t) gridDim.x * blockDim.x)
 	{
-		int iy = (int) (i / g.nx), ix = (int) (i - (int64_t) iy * g.nx);
+		int iy = (int) (i >> g.lnx), ix = (int) i & (g.nx - 1);
+		// rows 0..ny (row ny is the south ghost: row 0 again)
 		int y0 = iy - 1 < 0 ? g.ny - 1 : iy - 1;
-		int y1 = (iy + 1) % g.ny;
-		int yc = iy % g.ny;
-		int x0 = (ix + g.nx - 1) % g.nx;
-		int x1 = (ix + 1) % g.nx;
+		int y1 = (iy + 1) & (g.ny - 1);
+		int yc = iy & (g.ny - 1);
+		int x0 = (ix - 1) & (g.nx - 1);
+		int x1 = (ix + 1) & (g.nx - 1);
 		Ey[i] = (phi[(int64_t) y0 * g.nx + ix] - phi[(int64_t) y1 * g.nx + ix]) / dy2;
 		Ex[i] = (phi[(int64_t) yc * g.nx + x0] - phi[(int64_t) yc * g.nx + x1]) / dx2;
 	}

@@ -11,28 +11,39 @@ namespace cpic {
 // stored as (Ex, Ey) pairs for the per-tile shared-memory stage.
 __global__ void k_E_mix(Grid g, const float *phi, float2 *E)
 {
-	int64_t total = (int64_t) g.ny * g.nx;
-	float rdx2 = (float) (1.0 / (2 * g.dx)), rdy2 = (float) (1.0 / (2 * g.dy));
-	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
-			i += (int64_t) gridDim.x * blockDim.x)
+	// four nodes of one row per thread (nx is a power of two >= 4): one
+	// float4 of phi from each of the three rows, the two x neighbours
+	// outside it, two float4 stores of E
+	const int nq = g.nx >> 2;
+	const int64_t total = (int64_t) g.ny * nq;
+	const float rdx2 = (float) (1.0 / (2 * g.dx)), rdy2 = (float) (1.0 / (2 * g.dy));
+	for(int64_t q = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; q < total;
+			q += (int64_t) gridDim.x * blockDim.x)
 	{
-		int iy = (int) (i / g.nx), ix = (int) (i - (int64_t) iy * g.nx);
-		int y0 = iy == 0 ? g.ny - 1 : iy - 1;
-		int y1 = iy + 1 == g.ny ? 0 : iy + 1;
-		int x0 = ix == 0 ? g.nx - 1 : ix - 1;
-		int x1 = ix + 1 == g.nx ? 0 : ix + 1;
-		float2 e;
-		e.x = (phi[(int64_t) iy * g.nx + x0] - phi[(int64_t) iy * g.nx + x1]) * rdx2;
-		e.y = (phi[(int64_t) y0 * g.nx + ix] - phi[(int64_t) y1 * g.nx + ix]) * rdy2;
-		E[i] = e;
+		const int iy = (int) (q >> (g.lnx - 2)), x = ((int) q & (nq - 1)) << 2;
+		const int y0 = iy == 0 ? g.ny - 1 : iy - 1;
+		const int y1 = iy + 1 == g.ny ? 0 : iy + 1;
+		const float *r = phi + ((int64_t) iy << g.lnx);
+		const float4 c = *reinterpret_cast<const float4 *>(r + x);
+		const float4 u = *reinterpret_cast<const float4 *>(phi + ((int64_t) y0 << g.lnx) + x);
+		const float4 d = *reinterpret_cast<const float4 *>(phi + ((int64_t) y1 << g.lnx) + x);
+		const float l = r[(x - 1) & (g.nx - 1)], rr = r[(x + 4) & (g.nx - 1)];
+		float4 e0, e1;
+		e0.x = (l - c.y) * rdx2;   e0.y = (u.x - d.x) * rdy2;
+		e0.z = (c.x - c.z) * rdx2; e0.w = (u.y - d.y) * rdy2;
+		e1.x = (c.y - c.w) * rdx2; e1.y = (u.z - d.z) * rdy2;
+		e1.z = (c.z - rr) * rdx2;  e1.w = (u.w - d.w) * rdy2;
+		float4 *o = reinterpret_cast<float4 *>(E + ((int64_t) iy << g.lnx) + x);
+		o[0] = e0;
+		o[1] = e1;
 	}
 }
 
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s)
 {
-	int64_t total = (int64_t) g.ny * g.nx;
+	int64_t total = (int64_t) g.ny * (g.nx >> 2);
 	int blocks = (int) ((total + 255) / 256);
-	if(blocks > 4096) blocks = 4096;
+	if(blocks > 8 * 152) blocks = 8 * 152;
 	k_E_mix<<<blocks, 256, 0, s>>>(g, phi, E);
 }
 
@@ -127,7 +138,7 @@ void launch_spill_mix(const SpillArgs &a, cudaStream_t s)
 
 void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
-		const double *cosy, float *phi, cudaStream_t s, const float *Gt)
+		const double *cosy, float *phi, cudaStream_t s, const float *Gt, double mean0)
 {
 	static bool init = false;
 	if(!init)
@@ -137,7 +148,8 @@ void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const 
 		cudaFuncSetAttribute(k_rows_inv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 		init = true;
 	}
-	poisson_launch<float>(g, rho, qinv, mean, spec, twx, twy, cosx, cosy, phi, s, nullptr, 0.0, Gt);
+	poisson_launch<float>(g, rho, qinv, mean, spec, twx, twy, cosx, cosy, phi, s, nullptr, 0.0, Gt,
+			mean0);
 }
 
 } // namespace cpic
