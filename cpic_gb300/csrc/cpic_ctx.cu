@@ -60,6 +60,12 @@ struct cpic_ctx {
 	double qlo_mul, qinv_lo;  // FP64 form: remainder-word scales
 	bool wq_exact;            // mixed form: integer charge multiples
 	cudaStream_t stream;
+	// the tile fix-up of a step may run on `side`, overlapping the next
+	// step's field solve (which touches no particle); `stream` waits for
+	// ev_fix (join_fixup) before anything reads the particles again
+	cudaStream_t side;
+	cudaEvent_t ev_push, ev_fix;
+	bool fix_pending;
 	int nspecies;
 	SpeciesHost sp[kMaxSpecies];
 	int spill_cur;
@@ -878,7 +884,7 @@ static int rebuild_if_spilled(cpic_ctx *c)
 // One fused particle stage (gather, push, re-bin, deposit) without
 // host synchronisation.  deposit_only: the initial charge deposit.
 static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = nullptr,
-		cudaEvent_t ev1 = nullptr)
+		cudaEvent_t ev1 = nullptr, bool overlap = false)
 {
 	cudaStream_t st = c->stream;
 	int64_t ng = (int64_t) c->g.nx * c->g.ny;
@@ -921,13 +927,36 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 		launch_push_f64(sa.p, c->ntiles, smem, st);
 	if(ev1) CK(cudaEventRecord(ev1, st));
 	CK(cudaGetLastError());
+	// the tile fix-up: bandwidth-bound, so with `overlap` it runs on the
+	// side stream beside the next step's latency-bound field solve
+	cudaStream_t fs = st;
+	if(overlap)
+	{
+		CK(cudaEventRecord(c->ev_push, st));
+		CK(cudaStreamWaitEvent(c->side, c->ev_push, 0));
+		fs = c->side;
+	}
 	dim3 fg(c->ntiles, c->nspecies);
 	if(c->precision == CPIC_MIXED)
-		k_fixup<Mix><<<fg, 256, 0, st>>>(sa.p);
+		k_fixup<Mix><<<fg, 256, 0, fs>>>(sa.p);
 	else
-		k_fixup<F64><<<fg, 256, 0, st>>>(sa.p);
+		k_fixup<F64><<<fg, 256, 0, fs>>>(sa.p);
 	CK(cudaGetLastError());
+	if(overlap)
+	{
+		CK(cudaEventRecord(c->ev_fix, c->side));
+		c->fix_pending = true;
+	}
 	c->spill_cur ^= 1;
+	return CPIC_OK;
+}
+
+// The main stream waits for a fix-up left running on the side stream.
+static int join_fixup(cpic_ctx *c)
+{
+	if(!c->fix_pending) return CPIC_OK;
+	c->fix_pending = false;
+	CK(cudaStreamWaitEvent(c->stream, c->ev_fix, 0));
 	return CPIC_OK;
 }
 
@@ -1031,11 +1060,22 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	g.lnx = ilog2(g.nx); g.lny = ilog2(g.ny);
 	g.ltx = ilog2(T); g.lty = ilog2(TY);
 	c->ntiles = g.ntx * g.nty;
-	if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+	// the main stream at the highest priority: the field solve's blocks go
+	// ahead of the fix-up blocks still waiting on the low-priority side
+	int prio_lo = 0, prio_hi = 0;
+	cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+	if(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess
+			|| cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess
+			|| cudaEventCreateWithFlags(&c->ev_push, cudaEventDisableTiming) != cudaSuccess
+			|| cudaEventCreateWithFlags(&c->ev_fix, cudaEventDisableTiming) != cudaSuccess)
 	{
+		if(c->stream) cudaStreamDestroy(c->stream);
+		if(c->side) cudaStreamDestroy(c->side);
+		if(c->ev_push) cudaEventDestroy(c->ev_push);
 		delete c;
 		return CPIC_ECUDA;
 	}
+	c->fix_pending = false;
 	int64_t ng = (int64_t) g.nx * g.ny;
 	int64_t nh = g.nx / 2 + 1;
 	int r = CPIC_OK;
@@ -1130,6 +1170,7 @@ fail:
 CPIC_API void cpic_destroy(cpic_ctx_t *c)
 {
 	if(!c) return;
+	cudaStreamSynchronize(c->side);
 	cudaStreamSynchronize(c->stream);
 	for(int s = 0; s < c->nspecies; s++)
 	{
@@ -1147,6 +1188,9 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->green64); cudaFree(c->green32); cudaFree(c->mean);
 	cudaFree(c->status); cudaFree(c->scratch); cudaFree(c->counter); cudaFree(c->counter_pair);
 	if(c->stream) cudaStreamDestroy(c->stream);
+	if(c->side) cudaStreamDestroy(c->side);
+	if(c->ev_push) cudaEventDestroy(c->ev_push);
+	if(c->ev_fix) cudaEventDestroy(c->ev_fix);
 	delete c;
 }
 
@@ -1337,24 +1381,35 @@ CPIC_API int cpic_step(cpic_ctx_t *c)
 	return rebuild_if_spilled(c);
 }
 
-CPIC_API int cpic_run(cpic_ctx_t *c, int64_t nsteps)
+static int run_steps(cpic_ctx *c, int64_t nsteps)
 {
-	if(!c) return CPIC_EINVAL;
-	if(!c->prepared) return CPIC_ESTATE;
 	for(int64_t k = 0; k < nsteps; k++)
 	{
 		if(c->p.cycles > 0 && c->iter >= c->p.cycles) return CPIC_EDONE;
+		// this step's field solve overlaps the previous step's tile
+		// fix-up; the join orders it before this step's particle stage
 		int r = field_stage_async(c);
 		if(r) return r;
-		if((r = plasma_stage_async(c, false))) return r;
+		if((r = join_fixup(c))) return r;
+		if((r = plasma_stage_async(c, false, nullptr, nullptr, true))) return r;
 		c->iter++;
 		if((k & 7) == 7 || k + 1 == nsteps)
 		{
+			if((r = join_fixup(c))) return r;
 			if((r = check_status(c))) return r;
 			if((r = rebuild_if_spilled(c))) return r;
 		}
 	}
 	return CPIC_OK;
+}
+
+CPIC_API int cpic_run(cpic_ctx_t *c, int64_t nsteps)
+{
+	if(!c) return CPIC_EINVAL;
+	if(!c->prepared) return CPIC_ESTATE;
+	int r = run_steps(c, nsteps);
+	int rj = join_fixup(c);
+	return r ? r : rj;
 }
 
 CPIC_API int64_t cpic_iter(const cpic_ctx_t *c) { return c ? c->iter : -1; }
@@ -1637,9 +1692,13 @@ CPIC_API int cpic_time_steps(cpic_ctx_t *c, int64_t nsteps, double *ms_total, do
 		CK(cudaEventRecord(f0, st));
 		if((r = field_stage_async(c))) break;
 		CK(cudaEventRecord(f1, st));
-		if((r = plasma_stage_async(c, false, ev[2 + 2 * k], ev[2 + 2 * k + 1]))) break;
+		// the previous step's fix-up ran beside the field solve
+		if((r = join_fixup(c))) break;
+		if((r = plasma_stage_async(c, false, ev[2 + 2 * k], ev[2 + 2 * k + 1], true))) break;
 		c->iter++;
 	}
+	if(r == CPIC_OK) r = join_fixup(c);
+	else join_fixup(c);
 	CK(cudaEventRecord(ev[1], st));
 	CK(cudaEventSynchronize(ev[1]));
 	float tot = 0.0f;
