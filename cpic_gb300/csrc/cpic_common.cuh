@@ -16,8 +16,9 @@
 // FP64 form: each contribution w*(-q/e0) is rounded to a multiple of
 // 1/qscale and summed per tile in 64-bit shared memory.  Mixed form: the
 // weights w are rounded to multiples of 2^-kWeightBits and summed per tile
-// in 32-bit shared memory (folded into a 64-bit shadow before any sum can
-// wrap); the species charge multiplies the tile sums at the flush.
+// in 32-bit shared memory (added to global rho and restarted before any
+// sum can wrap, which a check every kCheckChunks chunks detects); the
+// species charge multiplies the tile sums at the flush.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
