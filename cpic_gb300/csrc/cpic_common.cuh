@@ -377,8 +377,8 @@ void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 
 void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
 // resident blocks per SM of the mixed fused kernel at this dynamic shared
-// memory (0 on error)
-int push_mix_blocks_per_sm(size_t smem);
+// memory, for a store with or without ids (0 on error)
+int push_mix_blocks_per_sm(size_t smem, bool ids);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
 void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,

@@ -1326,8 +1326,8 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 		int H = std::max(hmin, std::min((int) ceil(1.2 * D) + 1, c->g.tx));
 		if(c->precision == CPIC_MIXED)
 		{
-			int target = push_mix_blocks_per_sm(push_smem_h(c, hmin));
-			while(H > hmin && push_mix_blocks_per_sm(push_smem_h(c, H)) < target)
+			int target = push_mix_blocks_per_sm(push_smem_h(c, hmin), c->p.track_ids != 0);
+			while(H > hmin && push_mix_blocks_per_sm(push_smem_h(c, H), c->p.track_ids != 0) < target)
 				H--;
 		}
 		c->g.halo = H;
@@ -1731,7 +1731,7 @@ CPIC_API int cpic_layout_stats(const cpic_ctx_t *c, int64_t *out)
 	if(c->nspecies > 0)
 	{
 		if(c->precision == CPIC_MIXED)
-			out[3] = push_mix_blocks_per_sm(push_smem(c));
+			out[3] = push_mix_blocks_per_sm(push_smem(c), c->p.track_ids != 0);
 		else
 			out[3] = push_f64_blocks_per_sm(push_smem(c));
 	}

@@ -82,8 +82,10 @@ void launch_gather_mix_tiles(const Grid &g, const StoreMix &st, const int64_t *b
 static void push_mix_attrs()
 {
 	static const bool done = [] {
-		const void *fns[2] = {(const void *) k_push<Mix, Mix::kMinBlocks>,
-				(const void *) k_push<Mix, Mix::kHiBlocks>};
+		const void *fns[4] = {(const void *) k_push<Mix, Mix::kMinBlocks, false>,
+				(const void *) k_push<Mix, Mix::kHiBlocks, false>,
+				(const void *) k_push<Mix, Mix::kMinBlocks, true>,
+				(const void *) k_push<Mix, Mix::kHiBlocks, true>};
 		for(const void *f : fns)
 		{
 			cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -97,37 +99,50 @@ static void push_mix_attrs()
 
 // Whether the register-capped instance of the fused kernel reaches its
 // Mix::kHiBlocks resident blocks per SM with this much dynamic shared
-// memory (else the unconstrained instance runs).
-static bool push_mix_hi(size_t smem)
+// memory (else the unconstrained instance runs).  The ids and no-ids
+// instances of a block count use the same registers within a few.
+static bool push_mix_hi(size_t smem, bool ids)
 {
 	push_mix_attrs();
 	int hi = 0;
-	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, k_push<Mix, Mix::kHiBlocks>,
-			kPushThreads, smem) != cudaSuccess)
-		return false;
-	return hi >= Mix::kHiBlocks;
+	cudaError_t e = ids
+		? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, k_push<Mix, Mix::kHiBlocks, true>,
+				kPushThreads, smem)
+		: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, k_push<Mix, Mix::kHiBlocks, false>,
+				kPushThreads, smem);
+	return e == cudaSuccess && hi >= Mix::kHiBlocks;
 }
 
-int push_mix_blocks_per_sm(size_t smem)
+int push_mix_blocks_per_sm(size_t smem, bool ids)
 {
-	if(push_mix_hi(smem))
+	if(push_mix_hi(smem, ids))
 		return Mix::kHiBlocks;
 	int lo = 0;
-	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, k_push<Mix, Mix::kMinBlocks>,
-			kPushThreads, smem) != cudaSuccess)
-		return 0;
-	return lo;
+	cudaError_t e = ids
+		? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, k_push<Mix, Mix::kMinBlocks, true>,
+				kPushThreads, smem)
+		: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, k_push<Mix, Mix::kMinBlocks, false>,
+				kPushThreads, smem);
+	return e == cudaSuccess ? lo : 0;
 }
 
 void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 {
-	const bool hi = push_mix_hi(smem);
 	for(int sp = 0; sp < a.nspecies; sp++)
 	{
-		if(hi)
-			k_push<Mix, Mix::kHiBlocks><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
+		const PushArgs b = species_args(a, sp);
+		const bool ids = b.mix[0].id != nullptr;
+		const bool hi = push_mix_hi(smem, ids);
+		if(ids)
+		{
+			if(hi) k_push<Mix, Mix::kHiBlocks, true><<<ntiles, kPushThreads, smem, s>>>(b);
+			else k_push<Mix, Mix::kMinBlocks, true><<<ntiles, kPushThreads, smem, s>>>(b);
+		}
 		else
-			k_push<Mix, Mix::kMinBlocks><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
+		{
+			if(hi) k_push<Mix, Mix::kHiBlocks, false><<<ntiles, kPushThreads, smem, s>>>(b);
+			else k_push<Mix, Mix::kMinBlocks, false><<<ntiles, kPushThreads, smem, s>>>(b);
+		}
 	}
 }
 

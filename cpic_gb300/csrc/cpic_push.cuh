@@ -66,6 +66,13 @@ struct F64 {
 		st.id[i] = r.id;
 	}
 
+	// the FP64 store always keeps ids
+	template <bool kIds>
+	static __device__ __forceinline__ void store_t(const PushArgs &a, int s, int64_t i, const Rec &r)
+	{
+		store(a, s, i, r);
+	}
+
 	// Staged chunk layout: x, y, ux, uy (kChunk doubles each), id.
 	static __host__ __device__ __forceinline__ size_t stage_bytes(bool)
 	{
@@ -390,6 +397,18 @@ struct Mix {
 		if(st.id) st.id[i] = r.id;
 	}
 
+	// kIds: whether the store keeps ids, known at compile time (no branch
+	// in the fused kernel's write-back)
+	template <bool kIds>
+	static __device__ __forceinline__ void store_t(const PushArgs &a, int s, int64_t i, const Rec &r)
+	{
+		const StoreMix &st = a.mix[s];
+		st.cell[i] = r.cell;
+		st.ox[i] = r.ox; st.oy[i] = r.oy;
+		st.ux[i] = r.ux; st.uy[i] = r.uy;
+		if(kIds) st.id[i] = r.id;
+	}
+
 	// Staged chunk layout: cell, ox, oy, ux, uy (kChunk 32-bit words
 	// each) and, when ids are tracked, id.
 	static __host__ __device__ __forceinline__ size_t stage_bytes(bool ids)
@@ -669,7 +688,8 @@ struct Mix {
 
 // ============================================================== kernels
 
-template <class F, int MinBlocks = F::kMinBlocks>
+// Ids: whether the species' store keeps particle ids (always for F64).
+template <class F, int MinBlocks = F::kMinBlocks, bool Ids = true>
 __global__ void __launch_bounds__(kPushThreads, MinBlocks)
 k_push(const PushArgs a)
 {
@@ -692,7 +712,7 @@ k_push(const PushArgs a)
 	const int W = g.tx + 2 * H + 1;
 	const int tx0 = (t & (g.ntx - 1)) << g.ltx;
 	const int ty0 = (t >> (g.lnx - g.ltx)) << g.lty;
-	const bool ids = a.mix[s].id != nullptr;
+	const bool ids = Ids;
 	const size_t sb = F::stage_bytes(ids);
 	// bulk-copy destinations need 16-byte alignment; the host adds 128
 	// bytes of slack for this round-up.  An offset from smem (not a pointer
@@ -842,7 +862,7 @@ k_push(const PushArgs a)
 				}
 			}
 			if(at >= 0)
-				F::store(a, s, at, rec[k]);
+				F::template store_t<Ids>(a, s, at, rec[k]);
 			wb += __popc(bs[k]);
 		}
 	}
