@@ -193,26 +193,29 @@ template <> struct RecTile<Mix> {
 	}
 };
 
-// Upload counting sort, histogram: block-local counts (shared-memory
-// atomics, one global atomic per block and bin) of the bins (tile, sign of
-// ux).  The sort (k_rb_pass) places inside every tile the particles moving
-// left first and those moving right after them: warps then mostly hold
-// particles leaving towards the same neighbour from the first step on, as
-// the in-place re-bin makes them after a tile's population has been
-// renewed.  Blocks take contiguous ranges.  Shared memory: 2 nt ints.
+// Upload, step 1: every staged record converted once to the store's form
+// (the FP64 work of the upload, done once), in staging order, into a
+// temporary store, with its bucket key (ux >= 0 ? nt : 0) + tile in a key
+// column.  Block-local histograms (shared-memory atomics, one global atomic
+// per block and bin) give each tile's count and its count of left movers.
+// Blocks take contiguous ranges.  Shared memory: 2 nt ints.
 template <class F>
-__global__ void k_rb_count_blk(Grid g, Spill S, int64_t n, int nt, int32_t *cnt, int32_t *neg)
+__global__ void k_rb_convert(const PushArgs tmp, int s, Spill S, int64_t n, int nt, int32_t *key,
+		int32_t *cnt, int32_t *neg)
 {
 	extern __shared__ int32_t shb[];
+	const Grid &g = tmp.g;
 	for(int i = threadIdx.x; i < 2 * nt; i += blockDim.x) shb[i] = 0;
 	__syncthreads();
 	int64_t per = (n + gridDim.x - 1) / gridDim.x;
 	int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
 	for(int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
 	{
-		// the record as the sort sees it (the same tile and sign test)
 		typename F::Rec r = F::from_spill(S, k, g);
-		atomicAdd(&shb[(r.ux >= 0 ? nt : 0) + RecTile<F>::get(g, r)], 1);
+		const int kk = (r.ux >= 0 ? nt : 0) + RecTile<F>::get(g, r);
+		F::store(tmp, s, k, r);
+		key[k] = kk;
+		atomicAdd(&shb[kk], 1);
 	}
 	__syncthreads();
 	for(int t = threadIdx.x; t < nt; t += blockDim.x)
@@ -223,68 +226,199 @@ __global__ void k_rb_count_blk(Grid g, Spill S, int64_t n, int nt, int32_t *cnt,
 	}
 }
 
-// One pass of the upload sort.  Blocks take contiguous ranges of the input
-// and move it in batches of kRbPer x blockDim records: a shared histogram
-// ranks each record within its bucket, the first record of every bucket
-// reserves the batch's run at the bucket's cursor with one 64-bit global
-// atomic, and the records are written to their runs.  Every run is
-// contiguous and written within one batch, so its cache lines are whole
-// before they leave L2.  Pass 1 (from the FP64 staging list): buckets are
-// rows of tiles, output a temporary store grouped by row.  Pass 2 (from
-// that store): buckets are (direction of ux, tile), so inside every tile
-// the particles moving left come first; output the new layout.  Shared
-// memory: nb 64-bit offsets, then nb counters.
-constexpr int kRbPer = 4;
+// Upload, steps 2 and 3: the converted records move to per-bucket runs.
+// kRows: buckets are rows of tiles (output grouped by row); else buckets
+// are the keys themselves, (direction of ux, tile), so inside every tile
+// the particles moving left come first.  Blocks take contiguous ranges of
+// the input.  A block numbers the buckets its range can hold locally (all
+// rows in pass 1; in pass 2, whose input is grouped by row, the tiles of
+// the rows its range spans, in both directions), counts its records per
+// bucket from the key column, and reserves one run per bucket at the
+// bucket's cursor (one 64-bit global atomic per bucket and block).  Then,
+// per batch of kRbBatch records: a shared histogram and scan order the
+// batch by bucket in shared memory, and consecutive threads write
+// consecutive slots of each run, so the stores coalesce (scattering
+// records one by one left the passes 3 to 6 times slower than this).
+// A block whose range spans more than kRbMaxLocal buckets (very uneven
+// rows) stores record by record at the global cursors instead.
 constexpr int kRbThreads = 512;
+constexpr int kRbBatch = 2048;
+constexpr int kRbMaxLocal = 2048;
 
-template <class F, bool kFromStaging>
-__global__ void __launch_bounds__(kRbThreads)
-k_rb_pass(const PushArgs in, const PushArgs out, int s, Spill S, int64_t n, int nb,
-		unsigned long long *cursor)
+template <class F>
+constexpr size_t rb_smem_bytes()
 {
-	extern __shared__ __align__(8) unsigned char shraw[];
+	return (size_t) kRbMaxLocal * (8 + 4 + 4 + 4)
+		+ (size_t) kRbBatch * (4 + 4 + sizeof(typename F::Rec));
+}
+
+// Exclusive block-wide scan of v[0, n) into out (n <= 4 kRbThreads); ends
+// with a block barrier, so out[] is complete for every thread on return.
+__device__ __forceinline__ void rb_scan(const int32_t *v, int32_t *out, int n, int32_t *wsum)
+{
+	const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+	int a[4], sum = 0;
+	#pragma unroll
+	for(int k = 0; k < 4; k++)
+	{
+		const int i = 4 * t + k;
+		a[k] = i < n ? v[i] : 0;
+		sum += a[k];
+	}
+	int incl = sum;
+	for(int o = 1; o < 32; o <<= 1)
+	{
+		const int y = __shfl_up_sync(0xffffffffu, incl, o);
+		if(lane >= o) incl += y;
+	}
+	if(lane == 31) wsum[w] = incl;
+	__syncthreads();
+	if(w == 0)
+	{
+		int x = lane < kRbThreads / 32 ? wsum[lane] : 0;
+		int xi = x;
+		for(int o = 1; o < 32; o <<= 1)
+		{
+			const int y = __shfl_up_sync(0xffffffffu, xi, o);
+			if(lane >= o) xi += y;
+		}
+		if(lane < kRbThreads / 32) wsum[lane] = xi - x;
+	}
+	__syncthreads();
+	int run = wsum[w] + incl - sum;
+	#pragma unroll
+	for(int k = 0; k < 4; k++)
+	{
+		const int i = 4 * t + k;
+		if(i < n) out[i] = run;
+		run += a[k];
+	}
+	// every thread reads out[] of other threads next
+	__syncthreads();
+}
+
+template <class F, bool kRows>
+__global__ void __launch_bounds__(kRbThreads)
+k_rb_pass(const PushArgs in, const int32_t *kin, const PushArgs out, int32_t *kout, int s,
+		int64_t n, int nrow, unsigned long long *cursor, int64_t ncap_out)
+{
+	// every index below is in range by construction; the checks only turn
+	// a broken invariant into a status bit (ST_RANGE) instead of a stray
+	// access
+	typedef typename F::Rec Rec;
+	extern __shared__ __align__(16) unsigned char shraw[];
 	unsigned long long *off = reinterpret_cast<unsigned long long *>(shraw);
-	int32_t *hist = reinterpret_cast<int32_t *>(shraw + (size_t) nb * 8);
+	int32_t *run = reinterpret_cast<int32_t *>(off + kRbMaxLocal);
+	int32_t *bh = run + kRbMaxLocal;            // batch (or block) counts
+	int32_t *bs = bh + kRbMaxLocal;             // batch starts
+	int32_t *slb = bs + kRbMaxLocal;            // bucket of each staged slot
+	int32_t *skey = slb + kRbBatch;             // key of each staged slot
+	Rec *srec = reinterpret_cast<Rec *>(skey + kRbBatch);
+	__shared__ int32_t wsum[kRbThreads / 32];
 	const Grid &g = out.g;
 	const int nt = g.ntx * g.nty;
-	for(int i = threadIdx.x; i < nb; i += blockDim.x) hist[i] = 0;
-	__syncthreads();
+	const int ltxn = g.lnx - g.ltx, ntx = 1 << ltxn;
 	const int64_t per = (n + gridDim.x - 1) / gridDim.x;
 	const int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
-	for(int64_t b0 = lo; b0 < hi; b0 += (int64_t) kRbPer * blockDim.x)
+	if(lo >= hi) return;
+	// local buckets: pass 1 all rows; pass 2 the rows [r0, r0 + R) of
+	// this range (its input is grouped by row), left movers first
+	const int r0 = kRows ? 0 : (kin[lo] & (nt - 1)) >> ltxn;
+	const int R = kRows ? nrow : ((kin[hi - 1] & (nt - 1)) >> ltxn) - r0 + 1;
+	const int nbl = kRows ? nrow : 2 * R * ntx;
+	auto local = [&](int key) -> int {
+		const int tile = key & (nt - 1);
+		if(kRows) return tile >> ltxn;
+		return (key >= nt ? R * ntx : 0) + tile - (r0 << ltxn);
+	};
+	auto global = [&](int l) -> int {
+		if(kRows) return l;
+		const int right = l >= R * ntx;
+		return (right ? nt : 0) + (r0 << ltxn) + l - (right ? R * ntx : 0);
+	};
+	if(nbl > kRbMaxLocal)
 	{
-		typename F::Rec r[kRbPer];
-		int key[kRbPer], rank[kRbPer];
-		#pragma unroll
-		for(int k = 0; k < kRbPer; k++)
+		for(int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
 		{
-			const int64_t i = b0 + (int64_t) k * blockDim.x + threadIdx.x;
-			key[k] = -1;
-			rank[k] = 0;
-			if(i < hi)
+			const int key = kin[i];
+			const int gb = kRows ? (key & (nt - 1)) >> ltxn : key;
+			if(key < 0 || key >= 2 * nt) { set_status(out.status, ST_RANGE); continue; }
+			const int64_t dst = (int64_t) atomicAdd(&cursor[gb], 1ULL);
+			if(dst < 0 || dst >= ncap_out) { set_status(out.status, ST_RANGE); continue; }
+			F::store(out, s, dst, F::load(in, s, i));
+			if(kout) kout[dst] = key;
+		}
+		return;
+	}
+	for(int l = threadIdx.x; l < nbl; l += blockDim.x) bh[l] = 0;
+	__syncthreads();
+	for(int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+	{
+		const int l = local(kin[i]);
+		if(l >= 0 && l < nbl) atomicAdd(&bh[l], 1);
+		else set_status(out.status, ST_RANGE);
+	}
+	__syncthreads();
+	for(int l = threadIdx.x; l < nbl; l += blockDim.x)
+	{
+		const int c = bh[l];
+		if(c) off[l] = atomicAdd(&cursor[global(l)], (unsigned long long) c);
+		run[l] = 0;
+		bh[l] = 0;
+	}
+	__syncthreads();
+	constexpr int kPer = kRbBatch / kRbThreads;
+	for(int64_t b0 = lo; b0 < hi; b0 += kRbBatch)
+	{
+		const int m = (int) min((int64_t) kRbBatch, hi - b0);
+		int ll[kPer], rk[kPer], ky[kPer];
+		#pragma unroll
+		for(int k = 0; k < kPer; k++)
+		{
+			const int j = k * kRbThreads + threadIdx.x;
+			ll[k] = -1;
+			if(j < m)
 			{
-				if(kFromStaging)
-					r[k] = F::from_spill(S, i, g);
-				else
-					r[k] = F::load(in, s, i);
-				const int t = RecTile<F>::get(g, r[k]);
-				key[k] = kFromStaging ? t >> (g.lnx - g.ltx) : (r[k].ux >= 0 ? nt : 0) + t;
-				rank[k] = atomicAdd(&hist[key[k]], 1);
+				ky[k] = kin[b0 + j];
+				const int l = local(ky[k]);
+				if(l >= 0 && l < nbl)
+				{
+					ll[k] = l;
+					rk[k] = atomicAdd(&bh[l], 1);
+				}
 			}
 		}
 		__syncthreads();
+		rb_scan(bh, bs, nbl, wsum);                 // ends with a barrier
 		#pragma unroll
-		for(int k = 0; k < kRbPer; k++)
-			if(key[k] >= 0 && rank[k] == 0)
-				off[key[k]] = atomicAdd(&cursor[key[k]], (unsigned long long) hist[key[k]]);
-		__syncthreads();
-		#pragma unroll
-		for(int k = 0; k < kRbPer; k++)
-			if(key[k] >= 0)
+		for(int k = 0; k < kPer; k++)
+			if(ll[k] >= 0)
 			{
-				F::store(out, s, (int64_t) off[key[k]] + rank[k], r[k]);
-				hist[key[k]] = 0;
+				const int pos = bs[ll[k]] + rk[k];
+				if(pos < 0 || pos >= kRbBatch) { set_status(out.status, ST_RANGE); continue; }
+				slb[pos] = ll[k];
+				skey[pos] = ky[k];
+				srec[pos] = F::load(in, s, b0 + k * kRbThreads + threadIdx.x);
 			}
+		__syncthreads();
+		// slots in bucket order: consecutive threads, consecutive stores
+		// (the batch's valid records fill slots [0, mv))
+		const int mv = nbl > 0 ? bs[nbl - 1] + bh[nbl - 1] : 0;
+		for(int j = threadIdx.x; j < mv; j += blockDim.x)
+		{
+			const int l = slb[j];
+			if(l < 0 || l >= nbl) { set_status(out.status, ST_RANGE); continue; }
+			const int64_t dst = (int64_t) off[l] + run[l] + (j - bs[l]);
+			if(dst < 0 || dst >= ncap_out) { set_status(out.status, ST_RANGE); continue; }
+			F::store(out, s, dst, srec[j]);
+			if(kout) kout[dst] = skey[j];
+		}
+		__syncthreads();
+		for(int l = threadIdx.x; l < nbl; l += blockDim.x)
+		{
+			run[l] += bh[l];
+			bh[l] = 0;
+		}
 		__syncthreads();
 	}
 }
@@ -698,27 +832,39 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	else
 		CK(cudaMemcpyAsync(newcnt, S.tiles.cnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
 	bool mix = c->precision == CPIC_MIXED;
-	// the upload of a species: block-local counting sort by (tile, sign of ux)
+	// the upload of a species: one conversion pass (records, keys and the
+	// histogram of (tile, sign of ux)), then two sorting passes below
 	const bool blk = fresh && staging && nspill == 0 && nstage > 0 && nt <= kBlkSortMaxTiles;
 	const int blk_blocks = (int) std::min<int64_t>(152 * 8, (nstage + 4095) / 4096);
+	SpeciesHost tmp1, tmp2;
+	memset((void *) &tmp1, 0, sizeof(tmp1));
+	memset((void *) &tmp2, 0, sizeof(tmp2));
+	int32_t *key1 = nullptr, *key2 = nullptr;
 	if(blk)
 	{
 		static bool attr = false;
 		if(!attr)
 		{
-			const int mx = 4 * kBlkSortMaxTiles * (int) sizeof(int32_t);
-			cudaFuncSetAttribute(k_rb_count_blk<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			cudaFuncSetAttribute(k_rb_count_blk<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			const int mx = 2 * kBlkSortMaxTiles * (int) sizeof(int32_t);
+			cudaFuncSetAttribute(k_rb_convert<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			cudaFuncSetAttribute(k_rb_convert<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 			attr = true;
 		}
+		int r = alloc_store(c, tmp1, nstage, false);
+		if(r) return r;
+		CK(cudaMalloc(&key1, nstage * sizeof(int32_t)));
+		PushArgs t1 = make_args(c, c->spill_cur);
+		t1.f64[s] = tmp1.f64;
+		t1.mix[s] = tmp1.mix;
 		CK(cudaMalloc(&negcnt, nt * sizeof(int32_t)));
 		CK(cudaMemsetAsync(negcnt, 0, nt * sizeof(int32_t), st));
 		if(mix)
-			k_rb_count_blk<Mix><<<blk_blocks, 512, 2 * nt * sizeof(int32_t), st>>>(c->g, *staging,
-					nstage, nt, newcnt, negcnt);
+			k_rb_convert<Mix><<<blk_blocks, 512, 2 * nt * sizeof(int32_t), st>>>(t1, s, *staging,
+					nstage, nt, key1, newcnt, negcnt);
 		else
-			k_rb_count_blk<F64><<<blk_blocks, 512, 2 * nt * sizeof(int32_t), st>>>(c->g, *staging,
-					nstage, nt, newcnt, negcnt);
+			k_rb_convert<F64><<<blk_blocks, 512, 2 * nt * sizeof(int32_t), st>>>(t1, s, *staging,
+					nstage, nt, key1, newcnt, negcnt);
+		CK(cudaGetLastError());
 	}
 	else if(mix)
 	{
@@ -795,13 +941,14 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 			rowcur[r] = acc;
 			for(int t = r << ltxn; t < (r + 1) << ltxn; t++) acc += (unsigned long long) hc[t];
 		}
-		SpeciesHost tmp;
-		memset(&tmp, 0, sizeof(tmp));
-		int r = alloc_store(c, tmp, nstage, false);
+		int r = alloc_store(c, tmp2, nstage, false);
 		if(r) return r;
-		PushArgs tmpa = newa;
-		tmpa.f64[s] = tmp.f64;
-		tmpa.mix[s] = tmp.mix;
+		CK(cudaMalloc(&key2, nstage * sizeof(int32_t)));
+		PushArgs t1 = newa, t2 = newa;
+		t1.f64[s] = tmp1.f64;
+		t1.mix[s] = tmp1.mix;
+		t2.f64[s] = tmp2.f64;
+		t2.mix[s] = tmp2.mix;
 		unsigned long long *cur = nullptr;
 		CK(cudaMalloc(&cur, std::max(nrow, 2 * nt) * sizeof(unsigned long long)));
 		CK(cudaMemcpyAsync(cur, rowcur.data(), nrow * sizeof(unsigned long long),
@@ -809,29 +956,36 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 		static bool pattr = false;
 		if(!pattr)
 		{
-			const int mx = 2 * kBlkSortMaxTiles * 12;
-			cudaFuncSetAttribute(k_rb_pass<Mix, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			cudaFuncSetAttribute(k_rb_pass<F64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			cudaFuncSetAttribute(k_rb_pass<Mix, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			cudaFuncSetAttribute(k_rb_pass<F64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			const int mm = (int) rb_smem_bytes<Mix>(), mf = (int) rb_smem_bytes<F64>();
+			cudaFuncSetAttribute(k_rb_pass<Mix, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mm);
+			cudaFuncSetAttribute(k_rb_pass<F64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mf);
+			cudaFuncSetAttribute(k_rb_pass<Mix, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mm);
+			cudaFuncSetAttribute(k_rb_pass<F64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mf);
 			pattr = true;
 		}
 		const int pb = 152 * 2;
-		size_t sm1 = (size_t) nrow * 12, sm2 = (size_t) 2 * nt * 12;
+		const size_t smm = rb_smem_bytes<Mix>(), smf = rb_smem_bytes<F64>();
 		if(mix)
-			k_rb_pass<Mix, true><<<pb, kRbThreads, sm1, st>>>(tmpa, tmpa, s, *staging, nstage, nrow, cur);
+			k_rb_pass<Mix, true><<<pb, kRbThreads, smm, st>>>(t1, key1, t2, key2, s, nstage, nrow, cur,
+					nstage);
 		else
-			k_rb_pass<F64, true><<<pb, kRbThreads, sm1, st>>>(tmpa, tmpa, s, *staging, nstage, nrow, cur);
+			k_rb_pass<F64, true><<<pb, kRbThreads, smf, st>>>(t1, key1, t2, key2, s, nstage, nrow, cur,
+					nstage);
 		CK(cudaGetLastError());
 		k_rb_cursors<<<(nt + 255) / 256, 256, 0, st>>>(nt, nbase, negcnt, cur);
 		if(mix)
-			k_rb_pass<Mix, false><<<pb, kRbThreads, sm2, st>>>(tmpa, newa, s, *staging, nstage, 2 * nt, cur);
+			k_rb_pass<Mix, false><<<pb, kRbThreads, smm, st>>>(t2, key2, newa, nullptr, s, nstage,
+					nrow, cur, total);
 		else
-			k_rb_pass<F64, false><<<pb, kRbThreads, sm2, st>>>(tmpa, newa, s, *staging, nstage, 2 * nt, cur);
+			k_rb_pass<F64, false><<<pb, kRbThreads, smf, st>>>(t2, key2, newa, nullptr, s, nstage,
+					nrow, cur, total);
 		CK(cudaGetLastError());
 		CK(cudaStreamSynchronize(st));
 		cudaFree(cur);
-		free_store(c, tmp, false);
+		cudaFree(key1);
+		cudaFree(key2);
+		free_store(c, tmp1, false);
+		free_store(c, tmp2, false);
 		cudaFree(negcnt);
 	}
 	else if(mix)
