@@ -79,17 +79,23 @@ class ClockSampler:
 
     def __init__(self, index=0):
         self.index = index
-        self.samples = []
+        self.samples = []          # (host time, fields)
         self.proc = None
+        self.t0 = self.t1 = None
 
     def start(self):
+        """Starts sampling every 20 ms and waits (up to 5 s) for the first
+        reading, so that the sampler is live when the timed region starts."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t_end = time.perf_counter() + 5.0
+            while not self.samples and time.perf_counter() < t_end:
+                time.sleep(0.005)
         except Exception:
             self.proc = None
 
@@ -97,7 +103,13 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 7:
-                self.samples.append(parts)
+                self.samples.append((time.perf_counter(), parts))
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_end(self):
+        self.t1 = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
@@ -108,9 +120,17 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.thread.join(timeout=2)
+        # readings taken inside the timed region (host clock); if the region
+        # was shorter than the sampling interval, the first reading after
+        # its start
+        inside = [p for t, p in self.samples
+                  if self.t0 is not None and self.t0 <= t <= (self.t1 or t)]
+        if not inside:
+            after = [p for t, p in self.samples if self.t0 is None or t >= self.t0]
+            inside = after[:1]
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for p in self.samples:
+        for p in inside:
             try:
                 sm.append(float(p[0]))
                 mx = float(p[1])
@@ -120,7 +140,8 @@ class ClockSampler:
                 if p[3 + k].lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window_s": round(self.t1 - self.t0, 4) if self.t0 and self.t1 else None}
 
 
 def dist():
@@ -182,12 +203,16 @@ def run_ours(args):
     ctx = make_ctx(grid, st, prec, dt)
     ctx.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
     ctx.pre_step()
+    # the sampler goes live before the warm-up steps, which then keep the
+    # GPU busy up to the timed region
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
     if args.warmup:
         ctx.run(args.warmup)
     barrier()
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    clocks.start()
+    clocks.mark_start()
     t = ctx.time_steps(args.steps)
+    clocks.mark_end()
     clk = clocks.stop()
     ms_total = max_over_ranks(t["ms_total"])
     barrier()
