@@ -33,6 +33,7 @@ METRIC = "particle-steps/s on 1 GB300: FP32-offset vs FP64 plain at ≤1e-5 rel 
 UNIT = "particle-steps/s"
 B_P = {"mixed": 40.0, "fp64": 64.0}     # algorithmic bytes per particle-step
 B_G = {"mixed": 40.0, "fp64": 48.0}     # algorithmic bytes per grid node per step
+KERNELS_PER_STEP = 7                     # the benchmark workload has one species
 
 WORKLOADS = {
     # name: (grid, particles per cell, v0, vth, amp, description)
@@ -248,7 +249,9 @@ def run_ours(args):
                       "parallelism": "replicas" if ws > 1 else "single GPU"},
            "ms_breakdown": {"particle_kernel": push_ms, "field_stage": field_ms},
            "roofline": roof, "clocks": clk,
-           "gpu_launches": args.steps * (8 if form == "mixed" else 7)}
+           # per step, either form, one species: k_rows_fwd, k_cols, k_rows_inv,
+           # k_E_*, k_spill, k_push, k_fixup (and three memsets, not counted)
+           "gpu_launches": args.steps * KERNELS_PER_STEP}
 
     # ---- FP64 plain form on the same workload (speed-up and energy error)
     if form == "mixed" and not args.no_fp64:
