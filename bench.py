@@ -9,8 +9,9 @@ seeded init method.  The FP64 plain form runs the same workload for the
 speed-up and the field-energy error.
 
 One JSON line on rank 0.  `value` is device-resident throughput timed with
-CUDA events; `e2e` goes through the C ABI from host buffers (upload,
-pre-step, the steps with a per-step field-energy read-back, download).
+CUDA events; `e2e` goes through the C ABI from host buffers over the
+workload's whole run of 1000 steps (upload, pre-step, the steps with a
+per-step field-energy read-back, download).
 `--impl reference` times the oracle (the CPU restatement of the reference's
 FP64 step) on the host cores instead.
 """
@@ -653,7 +654,8 @@ def main():
     ap.add_argument("--ensemble-runs", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=400)
     ap.add_argument("--study-steps", type=int, default=1000)
-    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--e2e-steps", type=int, default=1000,
+                    help="steps of the end-to-end run: the workload's run length (1000 steps)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
