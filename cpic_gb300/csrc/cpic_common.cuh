@@ -71,6 +71,7 @@ struct Tiles {
 	int32_t *cnt;    // particles at the start of the step
 	int32_t *app;    // append cursor (starts at cnt)
 	int32_t *stay;   // stayers after the push
+	int32_t *order;  // tile taken by block b of the fused kernel (a permutation)
 };
 
 // Spill list: records that could not be placed in their tile.  Stored in

@@ -706,8 +706,15 @@ k_push(const PushArgs a)
 	// one launch per species, its data at index 0: every parameter access
 	// has a fixed offset (no indexed constant loads in the particle loop)
 	const int s = 0;
-	const int t = blockIdx.x;
 	const Tiles &T = a.tiles[s];
+	// blocks are dispatched in index order; the order array puts the
+	// heaviest tiles first (a permutation, so every tile is taken once)
+	const int t = T.order ? T.order[blockIdx.x] : (int) blockIdx.x;
+	if((unsigned) t >= gridDim.x)
+	{
+		if(threadIdx.x == 0) set_status(a.status, ST_RANGE);
+		return;
+	}
 	const int H = g.halo;
 	const int W = g.tx + 2 * H + 1;
 	const int tx0 = (t & (g.ntx - 1)) << g.ltx;
