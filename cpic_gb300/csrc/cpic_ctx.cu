@@ -124,11 +124,13 @@ __global__ void k_fixup(const PushArgs a)
 // group heaviest first in steps of 1/16 of the mean; the rest keep tile
 // order in between, so a uniform plasma keeps the identity order (and
 // neighbouring tiles, which write into each other's free tails, run
-// together).  One warp per species (blockIdx.x); a stable counting sort,
-// so the order is a function of the counts alone.  Which block takes
-// which tile changes no result.
+// together).  A stable counting sort, so the order is a function of the
+// counts alone.  Which block takes which tile changes no result.
 constexpr int kOrderKeys = 512;
-constexpr int kOrderMaxTiles = 65536;
+constexpr int kOrderMid = kOrderKeys - 1 - 255;      // bucket of the middle class
+constexpr int kOrderThreads = 1024;
+constexpr int kOrderMaxTiles = 8192;                 // larger layouts keep tile order
+constexpr int kOrderPer = kOrderMaxTiles / kOrderThreads;
 
 __device__ __forceinline__ int order_bucket(int32_t cnt, int ntiles, long long sum)
 {
@@ -143,28 +145,57 @@ __device__ __forceinline__ int order_bucket(int32_t cnt, int ntiles, long long s
 	return kOrderKeys - 1 - key;                 // larger keys first
 }
 
-__global__ void __launch_bounds__(32) k_tile_order(const PushArgs a, int ntiles)
+// One block of kOrderThreads per species: the counts are read once, in
+// parallel; a uniform layout (every tile in the middle class) writes the
+// identity at once; otherwise warp 0 scans the bucket counts and scatters
+// from the buckets kept in shared memory.
+__global__ void __launch_bounds__(kOrderThreads) k_tile_order(const PushArgs a, int ntiles)
 {
 	const Tiles &T = a.tiles[blockIdx.x];
+	__shared__ uint16_t s_b[kOrderMaxTiles];
 	__shared__ int32_t cur[kOrderKeys];
-	const int lane = threadIdx.x;
+	__shared__ long long s_part[kOrderThreads / 32];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	int32_t c[kOrderPer];
 	long long sum = 0;
-	for(int i = lane; i < ntiles; i += 32)
-		sum += T.cnt[i];
+	#pragma unroll
+	for(int k = 0; k < kOrderPer; k++)
+	{
+		const int i = k * kOrderThreads + tid;
+		c[k] = i < ntiles ? T.cnt[i] : 0;
+		sum += c[k];
+	}
 	for(int o = 16; o > 0; o >>= 1)
 		sum += __shfl_xor_sync(0xffffffffu, sum, o);
-	if(sum <= 0)
+	if(lane == 0)
+		s_part[warp] = sum;
+	for(int k = tid; k < kOrderKeys; k += kOrderThreads)
+		cur[k] = 0;
+	__syncthreads();
+	sum = 0;
+	for(int w = 0; w < kOrderThreads / 32; w++)
+		sum += s_part[w];
+	int moved = 0;
+	#pragma unroll
+	for(int k = 0; k < kOrderPer; k++)
 	{
-		for(int i = lane; i < ntiles; i += 32)
+		const int i = k * kOrderThreads + tid;
+		if(i < ntiles)
+		{
+			const int b = sum > 0 ? order_bucket(c[k], ntiles, sum) : kOrderMid;
+			s_b[i] = (uint16_t) b;
+			moved |= b != kOrderMid;
+			atomicAdd(&cur[b], 1);
+		}
+	}
+	if(!__syncthreads_or(moved))
+	{
+		for(int i = tid; i < ntiles; i += kOrderThreads)
 			T.order[i] = i;
 		return;
 	}
-	for(int k = lane; k < kOrderKeys; k += 32)
-		cur[k] = 0;
-	__syncwarp();
-	for(int i = lane; i < ntiles; i += 32)
-		atomicAdd(&cur[order_bucket(T.cnt[i], ntiles, sum)], 1);
-	__syncwarp();
+	if(warp != 0)
+		return;
 	// exclusive scan: lane l owns buckets [16 l, 16 l + 16)
 	constexpr int per = kOrderKeys / 32;
 	int loc = 0;
@@ -188,7 +219,7 @@ __global__ void __launch_bounds__(32) k_tile_order(const PushArgs a, int ntiles)
 	for(int i0 = 0; i0 < ntiles; i0 += 32)
 	{
 		const int i = i0 + lane;
-		const int b = i < ntiles ? order_bucket(T.cnt[i], ntiles, sum) : -1;
+		const int b = i < ntiles ? (int) s_b[i] : -1;
 		const unsigned peers = __match_any_sync(0xffffffffu, b);
 		const int pos = b >= 0 ? cur[b] + __popc(peers & lanemask_lt()) : 0;
 		__syncwarp();
@@ -1186,7 +1217,7 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 		k_fixup<F64><<<fg, 256, 0, fs>>>(sa.p);
 	// the next launch's tile order, from the counts the fix-up leaves
 	if(c->ntiles <= kOrderMaxTiles)
-		k_tile_order<<<c->nspecies, 32, 0, fs>>>(sa.p, c->ntiles);
+		k_tile_order<<<c->nspecies, kOrderThreads, 0, fs>>>(sa.p, c->ntiles);
 	CK(cudaGetLastError());
 	if(overlap)
 	{
