@@ -429,6 +429,44 @@ def _growth_rate(t, we):
     return 0.5 * slope
 
 
+def study_phases(args):
+    """Step time through the whole run of the workload (mixed form), in
+    blocks of 50 CUDA-event-timed steps, each followed by 10 steps with a
+    field-energy read-back after every step (host-timed), with the layout
+    statistics and the spread of tile counts (largest and 99th percentile
+    over the mean) at the end of each block.  The two-stream run goes
+    through a linear phase, then bunches (tile counts up to 3.6x the mean,
+    tile overflows, layout rebuilds) and mixes in velocity."""
+    from cpic_gb300 import _lib, build
+    build.build()
+    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
+    st = make_state(grid, ppc, v0, vth, amp)
+    ctx = make_ctx(grid, st, _lib.MIXED, 0.05)
+    ctx.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
+    del st
+    ctx.pre_step()
+    T = ctx.tile_info()["tile_x"]
+    rows, done, blk = [], 0, 50
+    while done < args.study_steps:
+        t = ctx.time_steps(blk)
+        done += blk
+        stats = ctx.layout_stats()
+        tc = ctx.cell_counts().astype(np.int64).reshape(grid // T, T, grid // T, T).sum(axis=(1, 3))
+        t1 = time.perf_counter()
+        for _ in range(10):
+            ctx.run(1)
+            ctx.field_energy()
+        ms_sync = (time.perf_counter() - t1) * 100
+        done += 10
+        rows.append({"step": done, "ms_step": t["ms_total"] / blk, "ms_push": t["ms_plasma"] / blk,
+                     "ms_field": t["ms_field"] / blk, "ms_step_synced": ms_sync, "stats": stats,
+                     "tile_max_over_mean": float(tc.max() / tc.mean()),
+                     "tile_p99_over_mean": float(np.quantile(tc, 0.99) / tc.mean()),
+                     "field_energy": ctx.field_energy()})
+    ctx.close()
+    return {"study": "phases", "workload": desc, "tile": T, "rows": rows}
+
+
 def study_accuracy(args):
     """Mixed form against the FP64 form on the same workload from the same
     initial state: field-energy error through the linear phase (steps
@@ -648,10 +686,11 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--accuracy-steps", type=int, default=300,
                     help="steps of the mixed-vs-FP64 field-energy comparison (linear phase)")
-    ap.add_argument("--study", default="", choices=["", "accuracy", "ensemble", "adjoint"],
+    ap.add_argument("--study", default="", choices=["", "accuracy", "ensemble", "adjoint", "phases"],
                     help="accuracy: long mixed-vs-FP64 run (growth rate, energy drift), no timing; "
                     "ensemble: batched independent runs in one CUDA graph; adjoint: gradient "
-                    "cost and finite-difference check")
+                    "cost and finite-difference check; phases: step time through the whole "
+                    "run (--study-steps), with layout statistics")
     ap.add_argument("--ensemble-runs", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=400)
     ap.add_argument("--study-steps", type=int, default=1000)
@@ -678,6 +717,8 @@ def main():
         out = study_ensemble(args) if rank == 0 else None
     elif args.study == "adjoint":
         out = study_adjoint(args) if rank == 0 else None
+    elif args.study == "phases":
+        out = study_phases(args) if rank == 0 else None
     else:
         out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if rank == 0 and out is not None:
