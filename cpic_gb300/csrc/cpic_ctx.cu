@@ -883,7 +883,10 @@ static void free_store(cpic_ctx *c, SpeciesHost &S, bool alt)
 	}
 }
 
-static int alloc_spill(Spill &S, int32_t capacity, int cell_units = 0)
+// The count is cleared on the caller's stream, ahead of the work it
+// queues there (the context's streams do not synchronise with the legacy
+// default stream).
+static int alloc_spill(Spill &S, int32_t capacity, cudaStream_t st, int cell_units = 0)
 {
 	S.capacity = capacity;
 	S.cell_units = cell_units;
@@ -893,7 +896,7 @@ static int alloc_spill(Spill &S, int32_t capacity, int cell_units = 0)
 	CK(cudaMalloc(&S.uy, (size_t) capacity * sizeof(double)));
 	CK(cudaMalloc(&S.id, (size_t) capacity * sizeof(int32_t)));
 	CK(cudaMalloc(&S.count, sizeof(int32_t)));
-	CK(cudaMemset(S.count, 0, sizeof(int32_t)));
+	CK(cudaMemsetAsync(S.count, 0, sizeof(int32_t), st));
 	return CPIC_OK;
 }
 
@@ -1541,7 +1544,7 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	// finite y, ux, uy; largest |u| component for the halo
 	Spill stg;
 	memset(&stg, 0, sizeof(stg));
-	if((r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1)))) return r;
+	if((r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1), st))) return r;
 	double vmax = 0.0;
 	if(n > 0)
 	{
@@ -1577,14 +1580,14 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	CK(cudaMalloc(&S.tiles.order, nt * sizeof(int32_t)));
 	k_iota<<<grid_blocks(nt), 256, 0, st>>>(nt, S.tiles.order);
 	CK(cudaGetLastError());
-	CK(cudaMemset(S.tiles.cnt, 0, nt * sizeof(int32_t)));
-	CK(cudaMemset(S.tiles.app, 0, nt * sizeof(int32_t)));
-	CK(cudaMemset(S.tiles.stay, 0, nt * sizeof(int32_t)));
+	CK(cudaMemsetAsync(S.tiles.cnt, 0, nt * sizeof(int32_t), st));
+	CK(cudaMemsetAsync(S.tiles.app, 0, nt * sizeof(int32_t), st));
+	CK(cudaMemsetAsync(S.tiles.stay, 0, nt * sizeof(int32_t), st));
 	// room for an eighth of the species to overflow between two host checks
 	int32_t scap = (int32_t) std::max<int64_t>(65536, n / 8);
 	const int cu = c->precision == CPIC_MIXED ? 1 : 0;
-	if((r = alloc_spill(S.spill[0], scap, cu))) return r;
-	if((r = alloc_spill(S.spill[1], scap, cu))) return r;
+	if((r = alloc_spill(S.spill[0], scap, st, cu))) return r;
+	if((r = alloc_spill(S.spill[1], scap, st, cu))) return r;
 	c->nspecies++;
 
 	// counting sort of the staged particles into the tiles
@@ -1749,11 +1752,11 @@ CPIC_API int cpic_set_particles(cpic_ctx_t *c, int s, const double *x, const dou
 	for(int64_t i = 0; i < n; i++)
 		if(!(x[i] >= 0.0 && x[i] <= c->p.Lx) || !(y[i] >= 0.0 && y[i] <= c->p.Ly))
 			return CPIC_EINVAL;
+	cudaStream_t st = c->stream;
 	Spill stg;
 	memset(&stg, 0, sizeof(stg));
-	int r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1));
+	int r = alloc_spill(stg, (int32_t) std::max<int64_t>(n, 1), st);
 	if(r) return r;
-	cudaStream_t st = c->stream;
 	if(n > 0)
 	{
 		CK(cudaMemcpyAsync(stg.x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
