@@ -66,6 +66,7 @@ struct cpic_ctx {
 	cudaStream_t side;
 	cudaEvent_t ev_push, ev_fix;
 	bool fix_pending;
+	int order_mode;           // tile order: 0 undecided, 1 computed each step, 2 kept
 	int nspecies;
 	SpeciesHost sp[kMaxSpecies];
 	int spill_cur;
@@ -1158,6 +1159,22 @@ static int rebuild_if_spilled(cpic_ctx *c)
 	return CPIC_OK;
 }
 
+// Whether ordering the tiles can shorten the fused kernel: only when its
+// blocks do not all fit on the GPU at once (more than one wave), and the
+// layout is small enough for the one-block sort.
+static bool tile_order_pays(const cpic_ctx *c, size_t smem)
+{
+	if(c->ntiles > kOrderMaxTiles)
+		return false;
+	int dev = 0, nsm = 0;
+	if(cudaGetDevice(&dev) != cudaSuccess
+			|| cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+		return true;
+	const int per_sm = c->precision == CPIC_MIXED
+		? push_mix_blocks_per_sm(smem, c->p.track_ids != 0) : push_f64_blocks_per_sm(smem);
+	return per_sm <= 0 || (int64_t) c->ntiles > (int64_t) per_sm * nsm;
+}
+
 // One fused particle stage (gather, push, re-bin, deposit) without
 // host synchronisation.  deposit_only: the initial charge deposit.
 static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = nullptr,
@@ -1219,7 +1236,9 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 	else
 		k_fixup<F64><<<fg, 256, 0, fs>>>(sa.p);
 	// the next launch's tile order, from the counts the fix-up leaves
-	if(c->ntiles <= kOrderMaxTiles)
+	if(c->order_mode == 0)
+		c->order_mode = tile_order_pays(c, smem) ? 1 : 2;
+	if(c->order_mode == 1)
 		k_tile_order<<<c->nspecies, kOrderThreads, 0, fs>>>(sa.p, c->ntiles);
 	CK(cudaGetLastError());
 	if(overlap)
