@@ -14,6 +14,11 @@ Fixtures (numpy .npz):
   harmonic.npz           conf/harmonic.conf (two electrons, 1024x1024):
                          x and E_x of particle 0 after each of 1200 steps,
                          from the reference build.
+  harmonic_line64.npz    the reference's own fixture test/harmonic/E.csv: the
+                         field of the same two electrons on the 64x64 grid
+                         (harmonic.conf's commented-out size) along the row
+                         y = 4 (64 points, x = 0 ... 7.875): E_x, E_y, phi,
+                         rho as exported, 6 significant digits.
 """
 import os
 import sys
@@ -37,7 +42,14 @@ def inputs(case):
     return d
 
 
-def main(which=("c1", "c2", "harmonic")):
+REF = "/root/reference"
+
+
+def main(which=("c1", "c2", "harmonic", "line")):
+    if "line" in which:
+        make_harmonic_line()
+        if which == ("line",):
+            return
     assert refrun.available(), "reference build unavailable"
     if "c1" in which:
         make_c1()
@@ -91,5 +103,13 @@ def make_harmonic():
     np.savez_compressed(os.path.join(HERE, "harmonic.npz"), x0=np.array(xs), Ex0=np.array(es))
 
 
+def make_harmonic_line():
+    # columns of E.csv: E_X, E_Y, Points_0, Points_1, Points_2,
+    # Points_Magnitude, phi, rho, Point ID
+    t = np.genfromtxt(os.path.join(REF, "test", "harmonic", "E.csv"), delimiter=",", skip_header=1)
+    np.savez_compressed(os.path.join(HERE, "harmonic_line64.npz"), Ex=t[:, 0], Ey=t[:, 1],
+                        x=t[:, 2], y=t[:, 3], phi=t[:, 6], rho=t[:, 7])
+
+
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]) or ("c1", "c2", "harmonic"))
+    main(tuple(sys.argv[1:]) or ("c1", "c2", "harmonic", "line"))
