@@ -7,7 +7,8 @@ TEST INFRASTRUCTURE.  MPI, FFTW and HDF5 are absent here, so the same
 single-rank shims as the oracle's reference build stand in for them
 (oracle/shims); libconfig is this project's parser.  Outputs go to
 tests/_dropin/ (git-ignored): cpic_gpu (src/cpic.c's main),
-test_constant_speed_gpu and test_cyclotron_gpu (test/*.c unchanged).
+test_constant_speed_gpu, test_cyclotron_gpu and test_harmonic_gpu (test/*.c
+unchanged).
 x86-64 only, because the reference uses AVX2 intrinsics.
 """
 import concurrent.futures as cf
@@ -27,7 +28,8 @@ CFLAGS = ["-std=gnu11", "-O2", "-ffp-contract=off", "-DNDEBUG", "-DUSE_VECTOR_25
           "-march=core-avx2", "-Wno-unknown-pragmas", "-w"]
 PROGRAMS = {"cpic_gpu": os.path.join(REF, "src", "cpic.c"),
             "test_constant_speed_gpu": os.path.join(REF, "test", "constant-speed.c"),
-            "test_cyclotron_gpu": os.path.join(REF, "test", "cyclotron.c")}
+            "test_cyclotron_gpu": os.path.join(REF, "test", "cyclotron.c"),
+            "test_harmonic_gpu": os.path.join(REF, "test", "harmonic.c")}
 
 
 def _run(cmd):

@@ -1,5 +1,5 @@
 """The drop-in sim layer (cpic_gb300/dropin/sim_gpu.c) against the
-reference's own callers: src/cpic.c and test/{constant-speed,cyclotron}.c
+reference's own callers: src/cpic.c and test/{constant-speed,cyclotron,harmonic}.c
 link unchanged against it and libcpic_gb300, with sim_init / sim_step /
 sim_run resolved from the drop-in.  Without a GPU, running them goes
 through the reference's whole host initialisation (config, species,
@@ -41,6 +41,7 @@ CONF = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
 
 @pytest.mark.parametrize("prog,conf", [("test_constant_speed_gpu", None),
                                        ("test_cyclotron_gpu", None),
+                                       ("test_harmonic_gpu", None),
                                        ("cpic_gpu", "conf/constant-speed.conf"),
                                        ("cpic_gpu", CONF)])
 def test_reference_callers_reach_gpu_library(out, prog, conf):
