@@ -554,6 +554,54 @@ def _member_ctx(m, precision, tile):
     return c, n
 
 
+def _oracle_member_step_s(m, timed=2):
+    """Seconds per step of the oracle on one ensemble member (same state
+    as _member_ctx), after its pre-step and one warm-up step."""
+    from oracle.oracle import Oracle
+    from cpic_gb300 import _lib
+    L = 2 * math.pi
+    n = m["grid"] * m["grid"] * m["ppc"]
+    x, y, ux, uy = _lib.init_two_stream(m["seed"], 0, n, L, L, m["v0"], 0.0, m["amp"])
+    q = -L * L / n
+    o = Oracle(m["grid"], m["grid"], L, L, 0.05, 1.0, (0.0, 0.0, 0.0))
+    o.add_species(q, -q, x, y, ux, uy)
+    o.pre_step()
+    o.step()
+    t0 = time.perf_counter()
+    for _ in range(timed):
+        o.step()
+    dt = (time.perf_counter() - t0) / timed
+    o.close()
+    return dt
+
+
+def ensemble_cpu_baseline(members, steps, threads):
+    """The ensemble on the host cores, one oracle process per run as the
+    reference would run it (one run per job): every member's cost per step
+    is timed on a bounded sample (2 steps after its pre-step and one
+    warm-up step, `threads` members at a time), scaled to `steps` steps,
+    and the runs are packed onto `threads` cores longest first."""
+    import heapq
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(threads) as pool:
+        per_step = pool.map(_oracle_member_step_s, members, chunksize=1)
+    sample_wall = time.perf_counter() - t0
+    work = sorted((steps * s for s in per_step), reverse=True)
+    cores = [0.0] * threads
+    for w in work:
+        heapq.heapreplace(cores, cores[0] + w)
+    makespan = max(cores)
+    return {"value": len(members) / makespan, "unit": "runs/s", "cores": threads, "kind": "port",
+            "seconds_estimated": makespan, "cpu_seconds": sum(work),
+            "sample": "oracle (FP64 C restatement of the reference step), one process per run on "
+                      "%d host cores: each run's step cost timed over 2 steps after its pre-step "
+                      "and one warm-up step (%.1f s wall for all %d runs), scaled to %d steps, runs "
+                      "packed onto the cores longest first" % (threads, sample_wall, len(members),
+                                                                steps)}
+
+
 def study_ensemble(args):
     """Batched ensemble: every run of the ensemble stepped by one CUDA graph
     (after autotuning the tile per (grid, particles per cell)), against the
@@ -626,6 +674,10 @@ def study_ensemble(args):
                                            "p90": float(np.quantile(errs, 0.9)),
                                            "max": float(errs.max()),
                                            "runs_below_1e-5": int(np.sum(errs <= 1e-5))}})
+    # the same runs on the host cores, one oracle process per run
+    if not args.no_cpu:
+        res["cpu_baseline"] = ensemble_cpu_baseline(members, steps, os.cpu_count() or 1)
+        res["runs_per_s_over_cpu"] = res["runs_per_s"] / res["cpu_baseline"]["value"]
     return res
 
 
