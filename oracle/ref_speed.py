@@ -8,7 +8,8 @@ for 1 and for 4 steps after its pre-step; the difference over 3 steps is its
 cost per step, with set-up and dumps cancelled. The oracle times the same
 3 steps directly.
 
-Usage: python oracle/ref_speed.py [grid] [particles per cell]  (needs the
+Usage: python oracle/ref_speed.py [grid] [particles per cell]
+       python oracle/ref_speed.py two_species                (needs the
 reference tree; test infrastructure, not part of the library)
 """
 import json
@@ -42,9 +43,9 @@ def reference_step_s(case, variant):
 
 def oracle_step_s(case):
     from oracle.oracle import Oracle
-    s = case["species"][0]
     o = Oracle(case["nx"], case["ny"], case["L"], case["L"], case["dt"], 1.0, case["B"])
-    o.add_species(s["q"], s["m"], s["x"], s["y"], s["ux"], s["uy"])
+    for s in case["species"]:
+        o.add_species(s["q"], s["m"], s["x"], s["y"], s["ux"], s["uy"])
     o.pre_step()
     o.step()
     t0 = time.perf_counter()
@@ -56,15 +57,21 @@ def oracle_step_s(case):
 
 
 def main():
-    grid = int(sys.argv[1]) if len(sys.argv) > 1 else 1024
-    ppc = int(sys.argv[2]) if len(sys.argv) > 2 else 10
     if not refrun.available():
         print(json.dumps({"unavailable": "the reference build (oracle/_ref) is not present"}))
         return
-    n = grid * grid * ppc
-    case = cases.two_stream(nx=grid, ny=grid, n=n, v0=0.2, vth=0.01, amp=0.01)
-    res = {"case": "two-stream %dx%d, %d electrons, dt 0.05" % (grid, grid, n), "particles": n,
-           "host": os.uname().machine, "cores": 1}
+    if len(sys.argv) > 1 and sys.argv[1] == "two_species":
+        # electrons and ions (mass ratio 100) in Bz = 0.5, 512x512, 16 per cell each
+        case = cases.two_species()
+        n = sum(len(s["x"]) for s in case["species"])
+        name = "two species 512x512, %d particles, Bz 0.5, dt 0.05" % n
+    else:
+        grid = int(sys.argv[1]) if len(sys.argv) > 1 else 1024
+        ppc = int(sys.argv[2]) if len(sys.argv) > 2 else 10
+        n = grid * grid * ppc
+        case = cases.two_stream(nx=grid, ny=grid, n=n, v0=0.2, vth=0.01, amp=0.01)
+        name = "two-stream %dx%d, %d electrons, dt 0.05" % (grid, grid, n)
+    res = {"case": name, "particles": n, "host": os.uname().machine, "cores": 1}
     for v in ("shipped", "exact"):
         t = reference_step_s(case, v)
         res["reference_" + v] = {"s_per_step": t, "particle_steps_per_s": n / t}
