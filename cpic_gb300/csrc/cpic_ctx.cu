@@ -118,8 +118,8 @@ __global__ void k_fixup(const PushArgs a)
 }
 
 // The order in which the next fused-kernel launch takes its tiles.  The
-// hardware dispatches blocks in index order, one block per tile, about 4.5
-// waves at the benchmark size; when the plasma bunches, a heavy tile
+// hardware dispatches blocks in index order, one block per tile (4096
+// tiles at 6 blocks per SM are about 4.5 waves); when the plasma bunches, a heavy tile
 // dispatched late leaves most SMs idle while it finishes.  So tiles above
 // 1.1x the mean count go first and tiles below 0.9x the mean go last, each
 // group heaviest first in steps of 1/16 of the mean; the rest keep tile
