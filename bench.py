@@ -180,6 +180,15 @@ def make_state(grid, ppc, v0, vth, amp, seed=2024):
 
 
 TILE = {"tile": 0, "halo": 0}
+DATA = "synthetic (seeded two-stream init, SplitMix64)"
+
+
+def bench_config(grid, ppc, desc):
+    """The workload's config, identical in both arms (precision goes in
+    dtype)."""
+    n = grid * grid * ppc
+    return {"workload": desc, "particles": n, "grid": [grid, grid], "dt": 0.05,
+            "l2": "inputs larger than L2 (particle state %.1f GB in the mixed form)" % (n * 20e-9)}
 
 
 def make_ctx(grid, st, precision, dt):
@@ -242,12 +251,9 @@ def run_ours(args):
            "scaling": "weak", "vs_baseline": None,
            "dtype": "f32 particle/field math, i32 cells, i64 fixed-point charge, f64 diagnostics"
            if form == "mixed" else "f64",
-           "data": "synthetic (seeded two-stream init, SplitMix64)",
-           "config": {"workload": desc + (", mixed precision" if form == "mixed" else ", FP64 plain"),
-                      "particles": n, "grid": [grid, grid], "dt": dt, "tile": tile,
-                      "l2": "inputs larger than L2 (particle state %.1f GB)" % (n * 20e-9 if form == "mixed"
-                                                                              else n * 36e-9),
-                      "parallelism": "replicas" if ws > 1 else "single GPU"},
+           "data": DATA, "config": bench_config(grid, ppc, desc),
+           "precision": "mixed" if form == "mixed" else "fp64 plain",
+           "tile": tile, "parallelism": "replicas" if ws > 1 else "single GPU",
            "ms_breakdown": {"particle_kernel": push_ms, "field_stage": field_ms},
            "roofline": roof, "clocks": clk,
            # per step, either form, one species: k_rows_fwd, k_cols, k_rows_inv,
@@ -255,29 +261,33 @@ def run_ours(args):
            # not counted)
            "gpu_launches": args.steps * KERNELS_PER_STEP}
 
-    # ---- FP64 plain form on the same workload (speed-up and energy error)
+    # ---- FP64 plain form on the same workload and the same window of the
+    # run (after the same warm-up): the speed-up against it
     if form == "mixed" and not args.no_fp64:
         ctx64 = make_ctx(grid, st, _lib.FP64, dt)
         ctx64.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
         ctx64.pre_step()
-        ctxm = make_ctx(grid, st, _lib.MIXED, dt)
-        ctxm.add_species(st["q"], st["m"], st["x"], st["y"], st["ux"], st["uy"])
-        ctxm.pre_step()
-        worst = 0.0
-        for k in range(args.accuracy_steps):
-            ctx64.step()
-            ctxm.step()
-            a, b = ctxm.field_energy(), ctx64.field_energy()
-            worst = max(worst, abs(a - b) / abs(b))
-        ctxm.close()
-        t64 = ctx64.time_steps(max(2, args.steps // 4))
-        ms64 = t64["ms_total"] / max(2, args.steps // 4)
+        if args.warmup:
+            ctx64.run(args.warmup)
+        k64 = max(2, args.steps // 4)
+        t64 = ctx64.time_steps(k64)
         ctx64.close()
+        ms64 = t64["ms_total"] / k64
         v64 = ws * n / (ms64 / 1e3)
-        out["fp64_plain"] = {"value": v64, "ms_per_step": ms64,
-                             "particle_kernel_ms": t64["ms_plasma"] / max(2, args.steps // 4)}
+        out["fp64_plain"] = {"value": v64, "ms_per_step": ms64, "steps": k64,
+                             "particle_kernel_ms": t64["ms_plasma"] / k64}
         out["speedup_vs_fp64"] = value / v64
-        out["we_rel_err_vs_fp64"] = {"steps": args.accuracy_steps, "max": worst}
+        # accuracy of the mixed form against the FP64 form, same initial
+        # state, through the whole run: field-energy error in the linear
+        # phase, growth rate and total-energy drift
+        if args.accuracy_steps > 0:
+            acc = accuracy_pair(grid, st, dt, args.accuracy_steps, args.linear_steps)
+            out["we_rel_err_vs_fp64"] = {"steps": acc["linear_steps"],
+                                         "max": acc["we_rel_err_max_linear"]}
+            out["accuracy_vs_fp64"] = {k: acc[k] for k in (
+                "steps", "linear_steps", "we_rel_err_max_linear", "we_rel_err_max_all",
+                "growth_window_steps", "growth_rate_fp64", "growth_rate_mixed", "growth_rate_rel_err",
+                "energy_drift_fp64", "energy_drift_mixed")}
 
     # ---- end to end through the C ABI with host buffers
     if not args.no_e2e:
@@ -308,9 +318,13 @@ def run_ours(args):
                       "path": "cpic_create/cpic_add_species/cpic_pre_step, per step cpic_run(1) + "
                               "cpic_field_energy read-back, cpic_get_particles"}
 
+    # ---- the FP64 plain form on the two-species Bz workload (GPU and oracle)
+    if rank == 0 and ws == 1 and not args.no_c2:
+        out["two_species_fp64"] = c2_record(args.warmup)
+
     # ---- CPU baseline: the oracle on a bounded sample of the workload
     if rank == 0 and ws == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(grid, ppc, v0, vth, amp, dt, n, threads=1)
+        out["cpu_baseline"] = cpu_baseline(grid, ppc, v0, vth, amp, dt, n)
     return out
 
 
@@ -332,92 +346,171 @@ def pinned_state(st, n):
         return {k: st[k] for k in ("x", "y", "ux", "uy")}, [np.empty(n) for _ in range(4)]
 
 
-def _oracle_sample(grid, ppc, v0, vth, amp, dt, frac, seed):
-    """Time the oracle on the full grid with a fraction of the particles;
-    returns (seconds per particle-step, seconds per field solve)."""
-    from oracle.oracle import Oracle
-    from cpic_gb300 import _lib
-    n = max(1024, int(grid * grid * ppc * frac))
+C2 = dict(grid=512, ppc=16, vth_e=0.05, mass_ratio=100.0, vth_i=0.005, Bz=0.5, dt=0.05, steps=500,
+          desc="two species 512x512, 16 electrons + 16 ions per cell (8,388,608 particles), "
+               "Maxwellian vth 0.05 / 0.005, mass ratio 100, Bz 0.5, dt 0.05, 500 steps, FP64 plain")
+
+
+def _c2_species(init):
+    """Electron and ion arrays of the two-species workload from an init
+    function with the (seed, species, n, Lx, Ly, vth) signature."""
     L = 2 * math.pi
-    x, y, ux, uy = _lib.init_two_stream(seed, 0, n, L, L, v0, vth, amp)
+    n = C2["grid"] ** 2 * C2["ppc"]
+    qe = -L * L / n
+    e = init(4321, 0, n, L, L, C2["vth_e"])
+    i = init(4321, 1, n, L, L, C2["vth_i"])
+    return [(qe, -qe, e), (-qe, -qe * C2["mass_ratio"], i)], n
+
+
+def c2_record(warmup):
+    """The FP64 plain form on the two-species Bz workload over its 500 steps
+    (CUDA events, after the iteration-0 half kick and `warmup` steps), beside
+    the oracle on one host core (full size, 1 warm-up + 2 timed steps)."""
+    from cpic_gb300 import _lib
+    L = 2 * math.pi
+    sp, n = _c2_species(_lib.init_maxwellian)
+    ctx = _lib.Context(C2["grid"], C2["grid"], L, L, C2["dt"], 1.0, (0.0, 0.0, C2["Bz"]),
+                       precision=_lib.FP64, track_ids=False)
+    for q, m, (x, y, ux, uy) in sp:
+        ctx.add_species(q, m, x, y, ux, uy)
+    del sp
+    ctx.pre_step()
+    ctx.run(1 + warmup)
+    t = ctx.time_steps(C2["steps"])
+    ctx.close()
+    total = 2 * n
+    v = total * C2["steps"] / (t["ms_total"] / 1e3)
+    # the oracle on the same state, one core
+    from oracle.oracle import Oracle, init_maxwellian
+    sp, _ = _c2_species(init_maxwellian)
+    o = Oracle(C2["grid"], C2["grid"], L, L, C2["dt"], 1.0, (0.0, 0.0, C2["Bz"]))
+    for q, m, (x, y, ux, uy) in sp:
+        o.add_species(q, m, x, y, ux, uy)
+    del sp
+    o.pre_step()
+    o.step()
+    o.step()
+    t0 = time.perf_counter()
+    o.step()
+    o.step()
+    cs = (time.perf_counter() - t0) / 2
+    o.close()
+    cpu = total / cs
+    return {"workload": C2["desc"], "particles": total, "value": v, "unit": UNIT,
+            "ms_per_step": t["ms_total"] / C2["steps"], "steps": C2["steps"],
+            "particle_kernel_ms": t["ms_plasma"] / C2["steps"],
+            "cpu_baseline": {"value": cpu, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "oracle on the full workload (8,388,608 particles), 1 warm-up "
+                                       "+ 2 timed steps after the half kick: %.3f s per step" % cs},
+            "speedup_vs_cpu_core": v / cpu}
+
+
+def _oracle_replica(grid, n, v0, vth, amp, dt, seed, warmup, steps, barrier=None, out=None):
+    """The oracle (FP64 C restatement of the reference's step) on the full
+    grid with n particles of the workload's seeded two-stream state: pre-step,
+    `warmup` untimed steps, then `steps` steps timed one by one on the host
+    clock, as the reference's own per-iteration timer does (sim.c:447-466).
+    Builds its input with the oracle's own init (no product library).  With
+    a barrier, every replica starts its timed steps together.  Returns (n,
+    t_start, t_end, per-step seconds, field-solve seconds per step)."""
+    from oracle.oracle import Oracle, init_two_stream
+    L = 2 * math.pi
+    x, y, ux, uy = init_two_stream(seed, 0, n, L, L, v0, vth, amp)
     q = -L * L / n
     o = Oracle(grid, grid, L, L, dt, 1.0, (0.0, 0.0, 0.0))
     o.add_species(q, -q, x, y, ux, uy)
+    del x, y, ux, uy
     o.pre_step()
-    o.step()
-    tf = tp = 0.0
-    steps = 2
+    for _ in range(warmup):
+        o.step()
+    if barrier is not None:
+        barrier.wait()
+    t_start = time.perf_counter()
+    per_step, field = [], []
     for _ in range(steps):
         t0 = time.perf_counter()
         o.stage_field_E()
         t1 = time.perf_counter()
         o.stage_plasma_E()
-        o.stage_plasma_r()
+        if o.stage_plasma_r():
+            raise RuntimeError("oracle step failed (velocity above umax)")
         o.stage_field_rho()
         o.iter = o.iter + 1
         t2 = time.perf_counter()
-        tf += t1 - t0
-        tp += t2 - t1
+        per_step.append(t2 - t0)
+        field.append(t1 - t0)
+    t_end = time.perf_counter()
     o.close()
-    return tp / (n * steps), tf / steps, n, steps
+    res = (n, t_start, t_end, per_step, statistics.mean(field))
+    if out is not None:
+        out.put(res)
+    return res
 
 
-def cpu_baseline(grid, ppc, v0, vth, amp, dt, n_full, threads=1):
+def cpu_baseline(grid, ppc, v0, vth, amp, dt, n_full):
+    """One core: the oracle on the full grid with 1/16 of the workload's
+    particles (all of them below 1024^2), 1 warm-up and 3 timed steps; the
+    per-particle cost and the field-solve cost are scaled to the workload."""
     frac = 1.0 / 16 if grid >= 1024 else 1.0
-    if threads <= 1:
-        cp, cg, ns, steps = _oracle_sample(grid, ppc, v0, vth, amp, dt, frac, 99)
-        per_step = n_full * cp + cg
-        return {"value": n_full / per_step, "unit": UNIT, "cores": 1, "kind": "port",
-                "sample": "oracle (FP64 C restatement of the reference step) on the full %dx%d grid "
-                          "with %d particles (1/%d of the workload), %d timed steps; particle cost "
-                          "%.1f ns/particle-step and field solve %.3f s/step scaled to %d particles"
-                          % (grid, grid, ns, round(1 / frac), steps, cp * 1e9, cg, n_full)}
-    import multiprocessing as mp
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(threads) as pool:
-        res = pool.starmap(_oracle_sample, [(grid, ppc, v0, vth, amp, dt, frac, 99 + i)
-                                            for i in range(threads)])
-    cp = statistics.mean(r[0] for r in res)
-    cg = statistics.mean(r[1] for r in res)
-    ns, steps = res[0][2], res[0][3]
-    per_step = n_full * cp + cg
-    # independent replicas on every core: aggregate throughput
-    return {"value": threads * n_full / per_step, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d concurrent oracle processes (FP64 C restatement of the reference step), each "
-                      "on the full %dx%d grid with %d particles (1/%d of the workload), %d timed "
-                      "steps; per-process cost %.1f ns/particle-step + %.3f s field solve per step, "
-                      "scaled to %d particles per replica"
-                      % (threads, grid, grid, ns, round(1 / frac), steps, cp * 1e9, cg, n_full)}
+    n = max(1024, int(n_full * frac))
+    n, t0, t1, per_step, tf = _oracle_replica(grid, n, v0, vth, amp, dt, 99, 1, 3)
+    tp = (statistics.mean(per_step) - tf) / n
+    per_full = n_full * tp + tf
+    return {"value": n_full / per_full, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "oracle (FP64 C restatement of the reference step) on the full %dx%d grid "
+                      "with %d particles (1/%d of the workload), 1 warm-up + 3 timed steps; particle "
+                      "cost %.1f ns/particle-step and field solve %.3f s/step scaled to %d particles"
+                      % (grid, grid, n, round(1 / frac), tp * 1e9, tf, n_full)}
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: one oracle process per
+    core, each on the full grid with 1/cores of the workload's particles (so
+    that together they step the workload's particle count), W warm-up steps,
+    then K steps timed together (a barrier starts them).  value = particles
+    stepped by all processes x K / wall time of that window.  Loads no
+    product library and uses no GPU."""
     ws, rank = dist()
-    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
     if rank != 0:
         return None
-    from cpic_gb300 import build
-    build.build()
+    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
     from oracle import oracle
     oracle.build()
-    threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    cb = cpu_baseline(grid, ppc, v0, vth, amp, 0.05, grid * grid * ppc, threads=threads)
-    el = time.perf_counter() - t0
-    v = cb["value"]
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    n_full = grid * grid * ppc
+    n = max(1024, n_full // cores)
+    ctx = mp.get_context("spawn")
+    barrier, q = ctx.Barrier(cores), ctx.Queue()
+    procs = [ctx.Process(target=_oracle_replica,
+                         args=(grid, n, v0, vth, amp, 0.05, 99 + i, args.warmup, args.steps, barrier, q))
+             for i in range(cores)]
+    for p in procs:
+        p.start()
+    res = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+        if p.exitcode != 0:
+            raise RuntimeError("oracle replica failed (exit code %s)" % p.exitcode)
+    window = max(r[2] for r in res) - min(r[1] for r in res)
+    total = sum(r[0] for r in res)
+    v = total * args.steps / window
+    ms_step = window / args.steps * 1e3
+    mean_step = statistics.mean(statistics.mean(r[3]) for r in res)
+    sample = ("%d concurrent oracle processes (FP64 C restatement of the reference step, single "
+              "threaded), one per host core, each the full %dx%d grid with %d of the workload's "
+              "particles (%d in all), %d warm-up + %d timed steps; mean step %.3f s per process, "
+              "of which %.3f s field solve" % (cores, grid, grid, n, total, args.warmup, args.steps,
+                                                mean_step, statistics.mean(r[4] for r in res)))
     return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": grid * grid * ppc / v * 1e3 / threads,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded two-stream init, SplitMix64)",
-            "config": {"workload": desc + ", FP64 (reference algorithm on host cores)",
-                       "particles": grid * grid * ppc, "grid": [grid, grid], "dt": 0.05},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"] + "; the reference's own sources build only "
-                             "on x86-64 (AVX2 intrinsics) against MPI/FFTW/libconfig stand-ins, "
-                             "so on this host its C restatement (pinned bit-exact to that build "
-                             "where it exists) runs"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_seconds": el}
+            "data": DATA, "config": bench_config(grid, ppc, desc),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample + "; the reference's own sources build only on x86-64 "
+                             "(AVX2 intrinsics) against MPI/FFTW/libconfig stand-ins, so its C "
+                             "restatement (pinned bit-exact to that build where it exists) runs"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def _growth_rate(t, we):
@@ -467,17 +560,13 @@ def study_phases(args):
     return {"study": "phases", "workload": desc, "tile": T, "rows": rows}
 
 
-def study_accuracy(args):
-    """Mixed form against the FP64 form on the same workload from the same
-    initial state: field-energy error through the linear phase (steps
-    0..linear_steps), growth rate of the field amplitude fitted in the linear
-    window, and the drift of the total energy (field + kinetic) over the
-    whole run."""
-    from cpic_gb300 import _lib, build
-    build.build()
-    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
-    dt = 0.05
-    st = make_state(grid, ppc, v0, vth, amp)
+def accuracy_pair(grid, st, dt, steps, lin):
+    """Mixed form against the FP64 form from the same initial state, `steps`
+    steps with the FP64 diagnostics after each: field-energy error through
+    the linear phase (steps 1..lin) and overall, growth rate of the field
+    amplitude fitted in the exponential window of the FP64 run, and the
+    drift of the total energy (field + kinetic) over the run."""
+    from cpic_gb300 import _lib
     ctx = {}
     for name, prec in (("fp64", _lib.FP64), ("mixed", _lib.MIXED)):
         c = make_ctx(grid, st, prec, dt)
@@ -485,19 +574,22 @@ def study_accuracy(args):
         c.pre_step()
         ctx[name] = c
     series = {k: {"we": [], "tot": []} for k in ctx}
-    for k in range(args.study_steps):
+    d0 = {name: c.diag() for name, c in ctx.items()}
+    for k in range(steps):
         for name, c in ctx.items():
             c.step()
             d = c.diag()
             series[name]["we"].append(d["WE"])
             series[name]["tot"].append(d["WE"] + d["KE"])
-    lin = min(args.accuracy_steps, args.study_steps)
+    for c in ctx.values():
+        c.close()
+    lin = min(lin, steps)
     we64 = np.array(series["fp64"]["we"])
     wem = np.array(series["mixed"]["we"])
     rel = np.abs(wem - we64) / we64
-    t = dt * np.arange(1, args.study_steps + 1)
+    t = dt * np.arange(1, steps + 1)
     # exponential phase of the FP64 run: from W_E rising above 10x its
-    # noise level (median over the first linear_steps) to 30% of its peak
+    # noise level (median over the first lin steps) to 30% of its peak
     base = float(np.median(we64[:lin]))
     above = np.nonzero(we64 > 10.0 * base)[0]
     top = np.nonzero(we64 >= 0.3 * we64.max())[0]
@@ -506,25 +598,36 @@ def study_accuracy(args):
     if i1 - i0 < 20:
         i0, i1 = max(1, lin // 6), lin
     win = slice(i0, i1)
-    res = {"study": "accuracy", "workload": desc, "steps": args.study_steps, "linear_steps": lin,
+    res = {"steps": steps, "linear_steps": lin,
            "we_rel_err_max_linear": float(rel[:lin].max()),
            "we_rel_err_max_all": float(rel.max()),
            "growth_window_steps": [win.start + 1, win.stop]}
     for name in ("fp64", "mixed"):
         we = np.array(series[name]["we"])
         tot = np.array(series[name]["tot"])
+        e0 = d0[name]["WE"] + d0[name]["KE"]
         res["growth_rate_" + name] = float(_growth_rate(t[win], we[win]))
-        res["energy_drift_" + name] = float((tot[-1] - tot[0]) / tot[0])
+        res["energy_drift_" + name] = float((tot[-1] - e0) / e0)
         res["we_final_" + name] = float(we[-1])
         res["we_max_" + name] = float(we.max())
     res["growth_rate_rel_err"] = abs(res["growth_rate_mixed"] - res["growth_rate_fp64"]) / abs(
         res["growth_rate_fp64"])
-    every = max(1, args.study_steps // 50)
-    res["we_samples"] = {"step": list(range(1, args.study_steps + 1, every)),
+    every = max(1, steps // 50)
+    res["we_samples"] = {"step": list(range(1, steps + 1, every)),
                          "fp64": [float(v) for v in we64[::every]],
                          "mixed": [float(v) for v in wem[::every]]}
-    for c in ctx.values():
-        c.close()
+    return res
+
+
+def study_accuracy(args):
+    """Mixed form against the FP64 form on the same workload from the same
+    initial state (accuracy_pair), no timing."""
+    from cpic_gb300 import build
+    build.build()
+    grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
+    st = make_state(grid, ppc, v0, vth, amp)
+    res = accuracy_pair(grid, st, 0.05, args.study_steps, args.linear_steps)
+    res.update({"study": "accuracy", "workload": desc})
     return res
 
 
@@ -557,11 +660,10 @@ def _member_ctx(m, precision, tile):
 def _oracle_member_step_s(m, timed=2):
     """Seconds per step of the oracle on one ensemble member (same state
     as _member_ctx), after its pre-step and one warm-up step."""
-    from oracle.oracle import Oracle
-    from cpic_gb300 import _lib
+    from oracle.oracle import Oracle, init_two_stream
     L = 2 * math.pi
     n = m["grid"] * m["grid"] * m["ppc"]
-    x, y, ux, uy = _lib.init_two_stream(m["seed"], 0, n, L, L, m["v0"], 0.0, m["amp"])
+    x, y, ux, uy = init_two_stream(m["seed"], 0, n, L, L, m["v0"], 0.0, m["amp"])
     q = -L * L / n
     o = Oracle(m["grid"], m["grid"], L, L, 0.05, 1.0, (0.0, 0.0, 0.0))
     o.add_species(q, -q, x, y, ux, uy)
@@ -736,8 +838,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="two_stream_2048", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--accuracy-steps", type=int, default=300,
-                    help="steps of the mixed-vs-FP64 field-energy comparison (linear phase)")
+    ap.add_argument("--accuracy-steps", type=int, default=1000,
+                    help="steps of the mixed-vs-FP64 comparison in the default line (the "
+                    "workload's run length; 0 skips it)")
+    ap.add_argument("--linear-steps", type=int, default=300,
+                    help="steps of the linear phase for the field-energy error bound")
     ap.add_argument("--study", default="", choices=["", "accuracy", "ensemble", "adjoint", "phases"],
                     help="accuracy: long mixed-vs-FP64 run (growth rate, energy drift), no timing; "
                     "ensemble: batched independent runs in one CUDA graph; adjoint: gradient "
@@ -751,6 +856,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-c2", action="store_true", help="skip the two-species FP64 record")
     ap.add_argument("--tile", type=int, default=0, help="tile size in cells (0: library default)")
     ap.add_argument("--halo", type=int, default=0, help="deposit halo in cells (0: library default)")
     args = ap.parse_args()

@@ -78,6 +78,7 @@ SIGNATURES = [
     ("cpic_cell_counts", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     ("cpic_diag", ctypes.c_int, [ctypes.c_void_p, D]),
     ("cpic_field_energy", ctypes.c_int, [ctypes.c_void_p, D]),
+    ("cpic_selftest_wait", ctypes.c_int, [ctypes.c_uint32]),
     ("cpic_status_bits", ctypes.c_uint32, [ctypes.c_void_p]),
     ("cpic_time_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, D, D, D]),
     ("cpic_tile_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),

@@ -714,18 +714,19 @@ CPIC_API int cpic_adj_create(const cpic_adj_params_t *p, int64_t n, cpic_adj_t *
 		}
 	}
 	{
-		static bool init = false;
-		if(!init)
+		static PerDeviceOnce once;
+		cudaError_t e = once.run([] {
+			return set_max_dyn_smem({(const void *) k_rows_fwd<double>, (const void *) k_cols<double>,
+					(const void *) k_rows_inv<double>, (const void *) k_rows_fwd_real<double>,
+					(const void *) k_rows_fwd<float>, (const void *) k_cols<float>,
+					(const void *) k_rows_inv<float>, (const void *) k_rows_fwd_real<float>},
+					200 * 1024);
+		});
+		if(e != cudaSuccess)
 		{
-			cudaFuncSetAttribute(k_rows_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(k_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(k_rows_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(k_rows_fwd_real<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(k_rows_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(k_cols<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(k_rows_inv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(k_rows_fwd_real<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			init = true;
+			fprintf(stderr, "cpic_adj_create: kernel set-up failed: %s\n", cudaGetErrorString(e));
+			r = CPIC_ECUDA;
+			goto fail;
 		}
 	}
 	if(cudaDeviceSynchronize() != cudaSuccess) { r = CPIC_ECUDA; goto fail; }

@@ -336,13 +336,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 	return ok != 0;
 }
 
+// Polls of a bounded mbarrier wait before it gives up (about 1.6 s with
+// the suspend hint above).
+constexpr uint32_t kWaitPolls = 1u << 14;
+
 // Wait for the mbarrier phase of the given parity, with an iteration limit:
 // on expiry the status word records ST_TIMEOUT and the caller goes on (its
 // indices are all clamped, so stale shared data cannot cause an
 // out-of-bounds access).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *status)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *status,
+		uint32_t polls = kWaitPolls)
 {
-	for(uint32_t it = 0; it < (1u << 14); it++)
+	for(uint32_t it = 0; it < polls; it++)
 		if(mbar_try_wait(bar, parity))
 			return true;
 	set_status(status, ST_TIMEOUT);
@@ -365,24 +370,73 @@ spill_push(const Spill &S, double x, double y, double ux, double uy, int32_t id)
 
 } // namespace cpic
 
-// Launchers implemented in the per-precision translation units.
+#include <initializer_list>
+#include <mutex>
+
 namespace cpic {
-void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
+
+// One-time set-up per CUDA device.  Kernel attributes such as the dynamic
+// shared-memory limit belong to the device that was current when they were
+// set, so a context created on another device needs them set again.  run(f)
+// calls f() the first time it is made with a given device current and
+// remembers success only: a failed f() is retried by the next call.
+class PerDeviceOnce {
+public:
+	template <class F> cudaError_t run(F f)
+	{
+		int dev = -1;
+		cudaError_t e = cudaGetDevice(&dev);
+		if(e != cudaSuccess) return e;
+		if(dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+		std::lock_guard<std::mutex> lk(m_);
+		if((done_ >> dev) & 1ull) return cudaSuccess;
+		e = f();
+		if(e == cudaSuccess) done_ |= 1ull << dev;
+		return e;
+	}
+
+private:
+	std::mutex m_;
+	unsigned long long done_ = 0;
+};
+
+// cudaFuncSetAttribute over a list of kernels; the first error, if any.
+inline cudaError_t set_max_dyn_smem(std::initializer_list<const void *> fns, int bytes,
+		bool carveout = false)
+{
+	for(const void *f : fns)
+	{
+		cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+		if(e == cudaSuccess && carveout)
+			e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+					cudaSharedmemCarveoutMaxShared);
+		if(e != cudaSuccess) return e;
+	}
+	return cudaSuccess;
+}
+
+} // namespace cpic
+
+// Launchers implemented in the per-precision translation units.  Those that
+// return cudaError_t report a failed one-time kernel set-up; launch errors
+// are left for the caller's cudaGetLastError.
+namespace cpic {
+cudaError_t launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
 int push_f64_blocks_per_sm(size_t smem);
 void launch_spill_f64(const SpillArgs &a, cudaStream_t s);
 void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s);
-void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
+cudaError_t launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
 		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo,
 		const double *Gt);
 
-void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
+cudaError_t launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
 // resident blocks per SM of the mixed fused kernel at this dynamic shared
 // memory, for a store with or without ids (0 on error)
 int push_mix_blocks_per_sm(size_t smem, bool ids);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
-void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,
+cudaError_t launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
 		const double *cosy, float *phi, cudaStream_t s, const float *Gt, double mean0 = 0.0);
 } // namespace cpic

@@ -1216,9 +1216,9 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 		launch_spill_f64(sa, st);
 	if(ev0) CK(cudaEventRecord(ev0, st));
 	if(c->precision == CPIC_MIXED)
-		launch_push_mix(sa.p, c->ntiles, smem, st);
+		CK(launch_push_mix(sa.p, c->ntiles, smem, st));
 	else
-		launch_push_f64(sa.p, c->ntiles, smem, st);
+		CK(launch_push_f64(sa.p, c->ntiles, smem, st));
 	if(ev1) CK(cudaEventRecord(ev1, st));
 	CK(cudaGetLastError());
 	// the tile fix-up: bandwidth-bound, so with `overlap` it runs on the
@@ -1271,14 +1271,14 @@ static int field_stage_async(cpic_ctx *c)
 		for(int s = 0; s < c->nspecies; s++)
 			tot += (double) c->sp[s].n * (-c->sp[s].q / c->p.e0);
 		double mean0 = tot / ((double) c->g.nx * (double) c->g.ny);
-		launch_poisson_mix(c->g, c->rho, c->qinv, nullptr, c->spec32, c->twx32, c->twy32,
-				c->cosx, c->cosy, c->phi32, st, c->green32, mean0);
+		CK(launch_poisson_mix(c->g, c->rho, c->qinv, nullptr, c->spec32, c->twx32, c->twy32,
+				c->cosx, c->cosy, c->phi32, st, c->green32, mean0));
 		launch_E_mix(c->g, c->phi32, c->E32, st);
 	}
 	else
 	{
-		launch_poisson_f64(c->g, c->rho, c->qinv, c->spec64, c->twx64, c->twy64,
-				c->cosx, c->cosy, c->phi64, st, c->rho_lo, c->qinv_lo, c->green64);
+		CK(launch_poisson_f64(c->g, c->rho, c->qinv, c->spec64, c->twx64, c->twy64,
+				c->cosx, c->cosy, c->phi64, st, c->rho_lo, c->qinv_lo, c->green64));
 		launch_E_f64(c->g, c->phi64, c->Ex64, c->Ey64, st);
 	}
 	CK(cudaGetLastError());
@@ -1974,6 +1974,49 @@ CPIC_API uint32_t cpic_status_bits(cpic_ctx_t *c)
 	cudaStreamSynchronize(c->stream);
 	cudaMemcpy(&st, c->status, sizeof(st), cudaMemcpyDeviceToHost);
 	return st;
+}
+
+// One warp waits on an mbarrier phase that cannot complete: thread 0 arms it
+// for 16 bytes of a bulk copy that is never issued, so no copy is in flight
+// and the wait can only expire.  The status word records ST_TIMEOUT.
+__global__ void k_wait_selftest(uint32_t polls, uint32_t *status)
+{
+	__shared__ __align__(8) uint64_t bar;
+	if(threadIdx.x == 0)
+	{
+		mbar_init(&bar, 1);
+		fence_mbar_init();
+	}
+	__syncthreads();
+	if(threadIdx.x == 0)
+		mbar_arrive_expect_tx(&bar, 16);
+	__syncwarp();
+	mbar_wait_bounded(&bar, 0, status, polls);
+}
+
+CPIC_API int cpic_selftest_wait(uint32_t polls)
+{
+	if(polls == 0 || polls > kWaitPolls) return CPIC_EINVAL;
+	int ndev = 0;
+	if(cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CPIC_ENODEV;
+	uint32_t *d = nullptr, st = 0;
+	cudaStream_t s = nullptr;
+	int r = CPIC_OK;
+	if(cudaMalloc((void **) &d, sizeof(uint32_t)) != cudaSuccess) return CPIC_ENOMEM;
+	if(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess
+			|| cudaMemsetAsync(d, 0, sizeof(uint32_t), s) != cudaSuccess)
+		r = CPIC_ECUDA;
+	if(r == CPIC_OK)
+	{
+		k_wait_selftest<<<1, 32, 0, s>>>(polls, d);
+		if(cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess
+				|| cudaMemcpy(&st, d, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess)
+			r = CPIC_ECUDA;
+	}
+	if(s) cudaStreamDestroy(s);
+	cudaFree(d);
+	if(r != CPIC_OK) return r;
+	return (st & ST_TIMEOUT) ? CPIC_ETIMEOUT : CPIC_OK;
 }
 
 CPIC_API int cpic_time_steps(cpic_ctx_t *c, int64_t nsteps, double *ms_total, double *ms_plasma,

@@ -115,6 +115,12 @@ __device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *
 	return a;
 }
 
+// The kernels below are static: the FP64 units (built without FMA
+// contraction) and the mixed and adjoint units (built with it) each get their
+// own copy, so a launch always runs the device code of the unit that makes
+// it, and a kernel attribute set in one unit leaves the other units' kernels
+// alone.
+
 // rho (fixed point, ny x nx) -> spec (ny x (nx/2+1)).  One block per row
 // pair.  value = (double) acc * qinv - mean, where the mean (the k = 0
 // mode, removed in FP64 before the FP32 transform of the mixed form, so
@@ -126,7 +132,7 @@ __device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *
 // reference).
 // rho_lo (FP64 form, may be null): the remainder word at scale qinv_lo.
 template <typename T>
-__global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, double qinv,
+static __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, double qinv,
 		const long long *rsum, typename Cx<T>::t *spec, const typename Cx<T>::t *tw,
 		const long long *rho_lo, double qinv_lo, double mean0)
 {
@@ -174,7 +180,7 @@ __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *rho, dou
 // Evaluated in FP64 from the same cosine tables and with the same
 // operations as k_cols's fallback below, so both give identical values.
 template <typename T>
-__global__ void k_green(int nx, int ny, const double *cosx, const double *cosy, T *Gt)
+static __global__ void k_green(int nx, int ny, const double *cosx, const double *cosy, T *Gt)
 {
 	int nh = nx / 2 + 1;
 	int64_t total = (int64_t) nh * ny;
@@ -192,7 +198,7 @@ __global__ void k_green(int nx, int ny, const double *cosx, const double *cosy, 
 // from the cosine tables (FP64 division per element: slow on a GPU with
 // few FP64 units, kept for callers without the table).
 template <typename T>
-__global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *spec,
+static __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *spec,
 		const typename Cx<T>::t *tw, const double *cosx, const double *cosy, const T *Gt)
 {
 	typedef typename Cx<T>::t C;
@@ -250,7 +256,7 @@ __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>::t *sp
 
 // spec -> phi (ny x nx real).  One block per row pair.
 template <typename T>
-__global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<T>::t *spec,
+static __global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<T>::t *spec,
 		const typename Cx<T>::t *tw, T *phi)
 {
 	typedef typename Cx<T>::t C;
@@ -292,7 +298,7 @@ __global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<T>::t *
 // Real-valued input (ny x nx of T) -> spec, otherwise as k_rows_fwd.  Used
 // by the adjoint, whose source term (rho-bar) is not a charge sum.
 template <typename T>
-__global__ void k_rows_fwd_real(int nx, int log2nx, const T *in, typename Cx<T>::t *spec,
+static __global__ void k_rows_fwd_real(int nx, int log2nx, const T *in, typename Cx<T>::t *spec,
 		const typename Cx<T>::t *tw)
 {
 	typedef typename Cx<T>::t C;

@@ -68,20 +68,19 @@ void launch_gather_f64_tiles(const Grid &g, const StoreF64 &st, const int64_t *b
 	k_gather_f64<<<ntiles, 256, 0, s>>>(g, st, base, cnt, Ex, Ey, ex_out, ey_out);
 }
 
-static void push_f64_attrs()
+static PerDeviceOnce g_push_f64_once, g_poisson_f64_once;
+
+static cudaError_t push_f64_attrs()
 {
-	static const bool done = [] {
-		cudaFuncSetAttribute(k_push<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(k_push<F64>, cudaFuncAttributePreferredSharedMemoryCarveout,
-				cudaSharedmemCarveoutMaxShared);
-		return true;
-	}();
-	(void) done;
+	return g_push_f64_once.run([] {
+		return set_max_dyn_smem({(const void *) k_push<F64>}, 200 * 1024, true);
+	});
 }
 
 int push_f64_blocks_per_sm(size_t smem)
 {
-	push_f64_attrs();
+	if(push_f64_attrs() != cudaSuccess)
+		return 0;
 	int b = 0;
 	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_push<F64>, kPushThreads, smem)
 			!= cudaSuccess)
@@ -89,11 +88,13 @@ int push_f64_blocks_per_sm(size_t smem)
 	return b;
 }
 
-void launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+cudaError_t launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 {
-	push_f64_attrs();
+	cudaError_t e = push_f64_attrs();
+	if(e != cudaSuccess) return e;
 	for(int sp = 0; sp < a.nspecies; sp++)
 		k_push<F64><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
+	return cudaSuccess;
 }
 
 void launch_spill_f64(const SpillArgs &a, cudaStream_t s)
@@ -101,21 +102,19 @@ void launch_spill_f64(const SpillArgs &a, cudaStream_t s)
 	k_spill<F64><<<152, kPushThreads, 0, s>>>(a);
 }
 
-void launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
+cudaError_t launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		double2 *spec, const double2 *twx, const double2 *twy, const double *cosx,
 		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo,
 		const double *Gt)
 {
-	static bool init = false;
-	if(!init)
-	{
-		cudaFuncSetAttribute(k_rows_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(k_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(k_rows_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		init = true;
-	}
+	cudaError_t e = g_poisson_f64_once.run([] {
+		return set_max_dyn_smem({(const void *) k_rows_fwd<double>, (const void *) k_cols<double>,
+				(const void *) k_rows_inv<double>}, 200 * 1024);
+	});
+	if(e != cudaSuccess) return e;
 	poisson_launch<double>(g, rho, qinv, nullptr, spec, twx, twy, cosx, cosy, phi, s, rho_lo, qinv_lo,
 			Gt);
+	return cudaSuccess;
 }
 
 } // namespace cpic

@@ -79,22 +79,16 @@ void launch_gather_mix_tiles(const Grid &g, const StoreMix &st, const int64_t *b
 	k_gather_mix<<<ntiles, 256, 0, s>>>(g, st, base, cnt, E, ex_out, ey_out);
 }
 
-static void push_mix_attrs()
+static PerDeviceOnce g_push_mix_once, g_poisson_mix_once;
+
+static cudaError_t push_mix_attrs()
 {
-	static const bool done = [] {
-		const void *fns[4] = {(const void *) k_push<Mix, Mix::kMinBlocks, false>,
+	return g_push_mix_once.run([] {
+		return set_max_dyn_smem({(const void *) k_push<Mix, Mix::kMinBlocks, false>,
 				(const void *) k_push<Mix, Mix::kHiBlocks, false>,
 				(const void *) k_push<Mix, Mix::kMinBlocks, true>,
-				(const void *) k_push<Mix, Mix::kHiBlocks, true>};
-		for(const void *f : fns)
-		{
-			cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-			cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
-					cudaSharedmemCarveoutMaxShared);
-		}
-		return true;
-	}();
-	(void) done;
+				(const void *) k_push<Mix, Mix::kHiBlocks, true>}, 200 * 1024, true);
+	});
 }
 
 // Whether the register-capped instance of the fused kernel reaches its
@@ -103,7 +97,8 @@ static void push_mix_attrs()
 // instances of a block count use the same registers within a few.
 static bool push_mix_hi(size_t smem, bool ids)
 {
-	push_mix_attrs();
+	if(push_mix_attrs() != cudaSuccess)
+		return false;
 	int hi = 0;
 	cudaError_t e = ids
 		? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, k_push<Mix, Mix::kHiBlocks, true>,
@@ -126,8 +121,10 @@ int push_mix_blocks_per_sm(size_t smem, bool ids)
 	return e == cudaSuccess ? lo : 0;
 }
 
-void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+cudaError_t launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 {
+	cudaError_t e = push_mix_attrs();
+	if(e != cudaSuccess) return e;
 	for(int sp = 0; sp < a.nspecies; sp++)
 	{
 		const PushArgs b = species_args(a, sp);
@@ -144,6 +141,7 @@ void launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
 			else k_push<Mix, Mix::kMinBlocks, false><<<ntiles, kPushThreads, smem, s>>>(b);
 		}
 	}
+	return cudaSuccess;
 }
 
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s)
@@ -151,20 +149,18 @@ void launch_spill_mix(const SpillArgs &a, cudaStream_t s)
 	k_spill<Mix><<<152, kPushThreads, 0, s>>>(a);
 }
 
-void launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *mean,
+cudaError_t launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *mean,
 		float2 *spec, const float2 *twx, const float2 *twy, const double *cosx,
 		const double *cosy, float *phi, cudaStream_t s, const float *Gt, double mean0)
 {
-	static bool init = false;
-	if(!init)
-	{
-		cudaFuncSetAttribute(k_rows_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(k_cols<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(k_rows_inv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		init = true;
-	}
+	cudaError_t e = g_poisson_mix_once.run([] {
+		return set_max_dyn_smem({(const void *) k_rows_fwd<float>, (const void *) k_cols<float>,
+				(const void *) k_rows_inv<float>}, 200 * 1024);
+	});
+	if(e != cudaSuccess) return e;
 	poisson_launch<float>(g, rho, qinv, mean, spec, twx, twy, cosx, cosy, phi, s, nullptr, 0.0, Gt,
 			mean0);
+	return cudaSuccess;
 }
 
 } // namespace cpic

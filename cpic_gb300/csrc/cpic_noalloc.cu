@@ -83,7 +83,10 @@ __global__ void k_noalloc_rows_fwd(int nx, int log2nx, const double *rho, double
 }
 
 // Device address of the scratch array for the current device, looked up
-// once per device.
+// once per device, together with the kernels' shared-memory limits (a
+// kernel attribute belongs to the device it was set on).  A device is marked
+// ready only when every step succeeded, so a failed set-up is retried by the
+// next call.
 static int scratch_for_current_device(void **out)
 {
 	int dev = -1;
@@ -94,19 +97,37 @@ static int scratch_for_current_device(void **out)
 	{
 		void *p = nullptr;
 		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-		if(e != cudaSuccess || !p)
+		if(e == cudaSuccess && !p)
+			e = cudaErrorInvalidSymbol;
+		// the largest blocks: two rows of kMaxN complex values, and two
+		// buffers of 128 KB of columns
+		if(e == cudaSuccess)
+			e = set_max_dyn_smem({(const void *) k_noalloc_rows_fwd,
+					(const void *) k_rows_inv<double>}, 2 * kMaxN * (int) sizeof(double2));
+		if(e == cudaSuccess)
+			e = set_max_dyn_smem({(const void *) k_cols<double>}, 2 * 128 * 1024);
+		if(e != cudaSuccess)
 		{
-			fprintf(stderr, "cpic_poisson_noalloc: cudaGetSymbolAddress failed: %s\n",
+			fprintf(stderr, "cpic_poisson_noalloc: set-up on device %d failed: %s\n", dev,
 					cudaGetErrorString(e));
 			return CPIC_ECUDA;
 		}
-		cudaFuncSetAttribute(k_noalloc_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-		cudaFuncSetAttribute(k_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		cudaFuncSetAttribute(k_rows_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
 		g_scratch_addr[dev] = p;
 	}
 	*out = g_scratch_addr[dev];
 	return CPIC_OK;
+}
+
+// One launch with its own error code (cudaLaunchKernel reports this launch's
+// configuration error, not an earlier one left pending on the thread).
+template <class T> struct same { typedef T type; };
+
+template <typename... A>
+static cudaError_t launch(void (*k)(A...), int blocks, int threads, size_t smem, cudaStream_t s,
+		typename same<A>::type... args)
+{
+	void *argv[] = {(void *) &args...};
+	return cudaLaunchKernel((const void *) k, dim3(blocks), dim3(threads), argv, smem, s);
 }
 
 } // namespace
@@ -138,17 +159,26 @@ cpic_poisson_noalloc(const double *rho, double *phi, int64_t nx, int64_t ny, voi
 	while((1 << log2nx) < nxi) log2nx++;
 	while((1 << log2ny) < nyi) log2ny++;
 
-	k_noalloc_tables<<<(kMaxN + 255) / 256, 256, 0, s>>>(nxi, nyi, twx, twy, cosx, cosy);
 	int rthreads = nxi / 2 < 32 ? 32 : (nxi / 2 > 512 ? 512 : nxi / 2);
-	k_noalloc_rows_fwd<<<nyi / 2, rthreads, 2 * (size_t) nxi * sizeof(double2), s>>>(
-			nxi, log2nx, rho, spec, twx);
 	int nh = nxi / 2 + 1;
 	int cb = (int) ((128 * 1024) / (2 * (size_t) nyi * sizeof(double2)));
 	if(cb < 1) cb = 1;
 	if(cb > nh) cb = nh;
-	k_cols<double><<<(nh + cb - 1) / cb, 512, 2 * (size_t) cb * nyi * sizeof(double2), s>>>(
-			nxi, nyi, log2ny, cb, spec, twy, cosx, cosy, nullptr);
-	k_rows_inv<double><<<nyi / 2, rthreads, 2 * (size_t) nxi * sizeof(double2), s>>>(
-			nxi, log2nx, nyi, spec, twx, phi);
-	return cudaGetLastError() == cudaSuccess ? CPIC_OK : CPIC_ECUDA;
+	const size_t rsm = 2 * (size_t) nxi * sizeof(double2);
+	const size_t csm = 2 * (size_t) cb * nyi * sizeof(double2);
+	cudaError_t e = launch(k_noalloc_tables, (kMaxN + 255) / 256, 256, 0, s, nxi, nyi, twx, twy,
+			cosx, cosy);
+	if(e == cudaSuccess)
+		e = launch(k_noalloc_rows_fwd, nyi / 2, rthreads, rsm, s, nxi, log2nx, rho, spec, twx);
+	if(e == cudaSuccess)
+		e = launch(k_cols<double>, (nh + cb - 1) / cb, 512, csm, s, nxi, nyi, log2ny, cb, spec, twy,
+				cosx, cosy, nullptr);
+	if(e == cudaSuccess)
+		e = launch(k_rows_inv<double>, nyi / 2, rthreads, rsm, s, nxi, log2nx, nyi, spec, twx, phi);
+	if(e != cudaSuccess)
+	{
+		fprintf(stderr, "cpic_poisson_noalloc: launch failed: %s\n", cudaGetErrorString(e));
+		return CPIC_ECUDA;
+	}
+	return CPIC_OK;
 }

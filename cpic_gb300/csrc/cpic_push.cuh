@@ -698,6 +698,7 @@ k_push(const PushArgs a)
 	__shared__ __align__(8) uint64_t bars[2];
 	__shared__ __align__(8) uint64_t ebars[2];
 	__shared__ int s_cursor;
+	__shared__ int s_timeout;        // a bounded wait of this block expired
 	// base and capacity of the 3 x 3 tiles around this one: nearly every
 	// mover lands there, so its slot needs no dependent global loads
 	__shared__ int64_t s_nbase[9];
@@ -748,6 +749,7 @@ k_push(const PushArgs a)
 	if(threadIdx.x == 0)
 	{
 		s_cursor = 0;
+		s_timeout = 0;
 		mbar_init(&bars[0], 1);          // "full": one arrival + bytes
 		mbar_init(&bars[1], 1);
 		mbar_init(&ebars[0], kPushThreads / 32);   // "empty": one per warp
@@ -779,8 +781,8 @@ k_push(const PushArgs a)
 		if(threadIdx.x == 0 && ci + 1 < nchunks)
 		{
 			const int b = (ci + 1) & 1;
-			if(ci >= 1)
-				mbar_wait_bounded(&ebars[b], ((ci - 1) >> 1) & 1, a.status);
+			if(ci >= 1 && !mbar_wait_bounded(&ebars[b], ((ci - 1) >> 1) & 1, a.status))
+				s_timeout = 1;
 			fence_proxy_async_smem();
 			F::stage_issue(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
 					stage0 + b * sb, &bars[b]);
@@ -788,7 +790,8 @@ k_push(const PushArgs a)
 		// this chunk has landed: every global read of slots below
 		// c0 + kChunk is complete, so the in-place writes below are safe
 		// (the stayer cursor never passes the end of the chunks read)
-		mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status);
+		if(!mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status))
+			s_timeout = 1;
 		const unsigned char *buf = stage0 + (ci & 1) * sb;
 		typename F::Rec rec[kPPT];
 		int dest[kPPT];
@@ -875,7 +878,19 @@ k_push(const PushArgs a)
 	}
 	__syncthreads();
 	if(threadIdx.x == 0)
+	{
 		T.stay[t] = s_cursor;
+		// after an expired wait a copy may still be landing in the stage:
+		// wait (bounded again) for the last one issued into each buffer
+		// before the block's shared memory is released
+		if(s_timeout)
+			for(int b = 0; b < 2; b++)
+			{
+				const int c = (nchunks - 1) - (((nchunks - 1) & 1) != b ? 1 : 0);
+				if(c >= 0)
+					mbar_wait_bounded(&bars[b], (c >> 1) & 1, a.status);
+			}
+	}
 	F::flush(a, s, fsm, W, H, tx0, ty0);
 }
 

@@ -162,6 +162,16 @@ CPIC_API int cpic_field_energy(cpic_ctx_t *ctx, double *out);
 /* Device status word (bit field, 0 = healthy) without clearing it. */
 CPIC_API uint32_t cpic_status_bits(cpic_ctx_t *ctx);
 
+/* No counterpart in the reference (it aborts instead of waiting).  Self-test
+ * of the device-side bounded wait that every kernel of this library uses
+ * on its shared-memory pipeline: one warp waits, with at most `polls` polls
+ * (each may suspend the thread up to 100 us; at most the kernels' own limit
+ * of 16384), on an mbarrier phase that never completes.  It is armed for
+ * the bytes of a copy that is never issued, so nothing is in flight.
+ * Returns CPIC_ETIMEOUT when the wait expired and the kernel returned, as it
+ * must; the device stays usable afterwards. */
+CPIC_API int cpic_selftest_wait(uint32_t polls);
+
 /* --- measurement ------------------------------------------------------ */
 
 /* Runs nsteps steps timed with CUDA events on the context's stream.

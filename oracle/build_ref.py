@@ -25,7 +25,7 @@ import platform
 import subprocess
 import sys
 
-REF = "/root/reference"
+REF = os.environ.get("CPIC_REFERENCE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_ref")

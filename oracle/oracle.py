@@ -66,6 +66,10 @@ def load():
         ("orc_cell_counts", None, [ctypes.c_void_p, I64]),
         ("orc_weights", None, [ctypes.c_double] * 6 + [D, I64]),
         ("orc_poisson", None, [ctypes.c_int64, ctypes.c_int64, D, D]),
+        ("orc_init_two_stream", None, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int64] + [ctypes.c_double] * 5
+         + [D] * 4),
+        ("orc_init_maxwellian", None, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int64] + [ctypes.c_double] * 5
+         + [D] * 4),
     ]
     for name, res, args in sig:
         fn = getattr(lib, name)
@@ -210,3 +214,20 @@ def poisson(rho):
     phi = np.empty_like(rho)
     lib.orc_poisson(nx, ny, _dp(rho), _dp(phi))
     return phi
+
+
+def init_two_stream(seed, species, n, Lx, Ly, v0, vth, amp):
+    """Seeded two-stream state (x, y, ux, uy), the same arrays as the
+    product's init method of that name."""
+    lib = load()
+    out = [np.empty(n) for _ in range(4)]
+    lib.orc_init_two_stream(seed, species, n, Lx, Ly, v0, vth, amp, *[_dp(a) for a in out])
+    return out
+
+
+def init_maxwellian(seed, species, n, Lx, Ly, vth, driftx=0.0, drifty=0.0):
+    """Seeded uniform positions with a drifting Maxwellian (x, y, ux, uy)."""
+    lib = load()
+    out = [np.empty(n) for _ in range(4)]
+    lib.orc_init_maxwellian(seed, species, n, Lx, Ly, vth, driftx, drifty, *[_dp(a) for a in out])
+    return out

@@ -42,7 +42,7 @@ def inputs(case):
     return d
 
 
-REF = "/root/reference"
+REF = os.environ.get("CPIC_REFERENCE", "/root/reference")
 
 
 def main(which=("c1", "c2", "harmonic", "line")):

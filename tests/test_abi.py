@@ -141,3 +141,21 @@ def test_two_stream_init_deterministic(lib):
     x, y, ux, uy = a
     assert ((x >= 0) & (x < L)).all() and ((y >= 0) & (y < L)).all()
     assert abs(ux[:500].mean() - 0.2) < 0.01 and abs(ux[500:].mean() + 0.2) < 0.01
+
+
+def test_oracle_init_matches_library_init(lib):
+    """The CPU legs of the benchmark build their inputs with the oracle's
+    restatement of the seeded init methods (so they load no product
+    library); it must give the product's arrays bit for bit."""
+    from oracle import oracle
+    L = 2 * np.pi
+    for args in ((2024, 0, 5001, L, L, 0.2, 0.01, 0.01), (3, 1, 777, L, 2 * L, 0.1, 0.0, 0.05),
+                 (9, 0, 640, L, L, 0.3, 0.02, 0.0)):
+        a = _lib.init_two_stream(*args)
+        b = oracle.init_two_stream(*args)
+        for u, v in zip(a, b):
+            assert np.array_equal(u, v)
+    a = _lib.init_maxwellian(11, 1, 3000, L, L, 0.05, 0.01, -0.02)
+    b = oracle.init_maxwellian(11, 1, 3000, L, L, 0.05, 0.01, -0.02)
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)

@@ -20,7 +20,7 @@ import pytest
 
 from tests import cases, refrun
 
-REF = "/root/reference"
+REF = os.environ.get("CPIC_REFERENCE", "/root/reference")
 pytestmark = pytest.mark.skipif(not os.path.isdir(REF) or not refrun.available(),
                                 reason="reference tree not present (development machine only)")
 
