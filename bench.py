@@ -59,17 +59,22 @@ def peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def profile_traffic(form):
-    """Per-particle DRAM traffic of the fused particle kernel from the
-    committed ncu summary (profiles/), or None."""
+def profile_value(key):
+    """A per-particle figure of the fused particle kernel from the committed
+    ncu summary (profiles/k_push_traffic.txt, `key: value` lines), or None."""
     path = os.path.join(ROOT, "profiles", "k_push_traffic.txt")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_particle_%s:" % form):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
+
+
+def profile_traffic(form):
+    """DRAM bytes per particle of the fused particle kernel, or None."""
+    return profile_value("traffic_bytes_per_particle_%s" % form)
 
 
 class ClockSampler:
@@ -276,6 +281,19 @@ def run_ours(args):
         v64 = ws * n / (ms64 / 1e3)
         out["fp64_plain"] = {"value": v64, "ms_per_step": ms64, "steps": k64,
                              "particle_kernel_ms": t64["ms_plasma"] / k64}
+        # its roofline: FP64 arithmetic (FLOPs per particle from the ncu
+        # instruction counts in profiles/) against the measured FP64 peak
+        fpp = profile_value("fp64_flops_per_particle")
+        try:
+            g64, _ = _lib.fp64_peak()
+        except Exception:
+            g64 = None
+        if fpp and g64:
+            ach = fpp * n / (out["fp64_plain"]["particle_kernel_ms"] / 1e3) / 1e9
+            out["fp64_plain"]["roofline"] = {
+                "bound": "fp64", "achieved": round(ach, 1), "peak": round(g64, 1), "unit": "GFLOP/s",
+                "frac": round(ach / g64, 4), "peak_kind": "measured (cpic_fp64_peak: FP64 FMA chains)",
+                "kernel": "k_push<F64>", "flops_per_particle": fpp}
         out["speedup_vs_fp64"] = value / v64
         # accuracy of the mixed form against the FP64 form, same initial
         # state, through the whole run: field-energy error in the linear

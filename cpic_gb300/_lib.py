@@ -79,6 +79,7 @@ SIGNATURES = [
     ("cpic_diag", ctypes.c_int, [ctypes.c_void_p, D]),
     ("cpic_field_energy", ctypes.c_int, [ctypes.c_void_p, D]),
     ("cpic_selftest_wait", ctypes.c_int, [ctypes.c_uint32]),
+    ("cpic_fp64_peak", ctypes.c_int, [ctypes.c_int64, D, D]),
     ("cpic_status_bits", ctypes.c_uint32, [ctypes.c_void_p]),
     ("cpic_time_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, D, D, D]),
     ("cpic_tile_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
@@ -386,3 +387,13 @@ def autotune_tile(nx, ny, Lx, Ly, dt, n, v0, vth, precision=MIXED, e0=1.0):
     if r < 0:
         raise CpicError(r, "cpic_autotune_tile")
     return t.value, ms.value
+
+
+def fp64_peak(iters=1 << 16):
+    """Measured FP64 GFLOP/s of the current device (cpic_fp64_peak)."""
+    lib = load()
+    g, ms = ctypes.c_double(), ctypes.c_double()
+    r = lib.cpic_fp64_peak(iters, ctypes.byref(g), ctypes.byref(ms))
+    if r < 0:
+        raise CpicError(r, "cpic_fp64_peak")
+    return g.value, ms.value

@@ -27,6 +27,7 @@ UNITS = [
     ("cpic_mixed.cu", ["--fmad=true"]),
     ("cpic_noalloc.cu", ["--fmad=false"]),
     ("cpic_adjoint.cu", ["--fmad=true"]),
+    ("cpic_peak.cu", ["--fmad=true"]),
 ]
 C_UNITS = ["cpic_init.c", "cpic_conf.c"]
 

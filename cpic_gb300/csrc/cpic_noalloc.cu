@@ -99,13 +99,13 @@ static int scratch_for_current_device(void **out)
 		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
 		if(e == cudaSuccess && !p)
 			e = cudaErrorInvalidSymbol;
-		// the largest blocks: two rows of kMaxN complex values, and two
-		// buffers of 128 KB of columns
+		// the largest blocks: two rows of kMaxN complex values, and the
+		// columns' two buffers of at most 128 KB together
 		if(e == cudaSuccess)
 			e = set_max_dyn_smem({(const void *) k_noalloc_rows_fwd,
 					(const void *) k_rows_inv<double>}, 2 * kMaxN * (int) sizeof(double2));
 		if(e == cudaSuccess)
-			e = set_max_dyn_smem({(const void *) k_cols<double>}, 2 * 128 * 1024);
+			e = set_max_dyn_smem({(const void *) k_cols<double>}, 128 * 1024);
 		if(e != cudaSuccess)
 		{
 			fprintf(stderr, "cpic_poisson_noalloc: set-up on device %d failed: %s\n", dev,

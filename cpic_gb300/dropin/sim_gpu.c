@@ -59,12 +59,15 @@
 #include "perf.h"
 #include "plasma.h"
 #include "plist.h"
+#include "solver.h"
 #include "specie.h"
 
 #include "cpic_gpu.h"
 
-/* Per-sim state of the GPU side, keyed by the sim_t pointer (sim_t has no
- * spare field; solver_t * is unused because the GPU owns the solver). */
+/* Per-sim state of the GPU side.  sim_t has no spare field, so it hangs off
+ * the sim's solver: sim->solver is a real solver_t (method "MFT", no FFTW
+ * plans: the GPU library owns the solve) whose `data` member, the slot the
+ * reference keeps for a solver's own state (solver.h:41), points here. */
 struct gpu_sim
 {
 	cpic_ctx_t *ctx;
@@ -74,9 +77,12 @@ struct gpu_sim
 	double *buf;            /* 4 * max(n) doubles: x y ux uy */
 	double *ebuf;           /* 2 * sum(n) doubles: E at the particles */
 	double *fbuf;           /* 2 * nx * (ny + 1) doubles */
+	int views_due;          /* host views are refreshed by this step's stages */
+	int e_pending;          /* ebuf holds E gathered before this step's push */
+	int err;                /* a stage failed: later stages and sim_step fail too */
 };
 
-#define GPU(sim) ((struct gpu_sim *) (sim)->solver)
+#define GPU(sim) ((sim)->solver ? (struct gpu_sim *) (sim)->solver->data : NULL)
 
 static void
 gpu_err(const char *what, int rc)
@@ -415,7 +421,13 @@ gpu_setup(sim_t *sim)
 	int64_t nmax = 1;
 
 	if(!g) return 1;
-	sim->solver = (solver_t *) g;
+	sim->solver = calloc(1, sizeof(solver_t));
+	if(!sim->solver) return 1;
+	sim->solver->method = METHOD_MFT;
+	sim->solver->dim = sim->dim;
+	sim->solver->nx = sim->ntpoints[X];
+	sim->solver->ny = sim->ntpoints[Y];
+	sim->solver->data = g;
 
 	memset(&p, 0, sizeof(p));
 	p.nx = sim->ntpoints[X];
@@ -554,46 +566,156 @@ sampling_done(sim_t *sim)
 	return 1.96 * sem < sim->stop_SEM * mean;
 }
 
+/* ---------------------------------------------------------------------
+ * Stage entry points, with the reference's prototypes (field.h:9-12,
+ * particle.h:20-26, mover.h:4, comm.h:38).  The GPU fuses the gather, the
+ * push with the periodic re-bin and the deposit into one kernel, so:
+ *
+ *   stage_field_E    rho -> phi -> E on the GPU (field.c:451); refreshes the
+ *                    host field views when they are due or when output is
+ *                    enabled (sim_step then calls the reference's
+ *                    output_fields, as sim.c:507 does);
+ *   stage_plasma_E   E at the particles (particle.c:233): on the GPU this is
+ *                    part of the next stage; when host views are due it
+ *                    gathers E at the pre-push positions into the ppacks'
+ *                    E, as the reference leaves it;
+ *   stage_plasma_r   the fused gather + Boris push + wrap + re-bin + charge
+ *                    deposit (mover.c:332 with comm_plasma, and the deposit
+ *                    of field.c:269);
+ *   stage_field_rho  the deposit is already done: refreshes the host views
+ *                    of rho and of the particles when they are due;
+ *   comm_plasma, particle_comm_initial
+ *                    the re-bin is part of stage_plasma_r and of the
+ *                    pre-step; nothing is left to exchange (one process).
+ *
+ * Host views are due on steps that are multiples of gpu.host_sync.  The
+ * reference aborts on a failing stage; the void stages here print the
+ * status and set a sticky error that makes every later stage a no-op and
+ * sim_step return -1.  A caller that runs the stages itself, as sim_step
+ * does, advances sim->iter after stage_field_rho.
+ * --------------------------------------------------------------------- */
+
+static int
+views_due(sim_t *sim, struct gpu_sim *g)
+{
+	return g->host_sync > 0 && (sim->iter % g->host_sync) == 0;
+}
+
+int
+stage_field_E(sim_t *sim)
+{
+	struct gpu_sim *g = GPU(sim);
+	int rc;
+	if(!g || g->err) return -1;
+	g->views_due = views_due(sim, g);
+	if((rc = cpic_stage_field_E(g->ctx)))
+	{
+		gpu_err("cpic_stage_field_E", rc);
+		g->err = rc;
+		return -1;
+	}
+	if((g->views_due || sim->output->enabled) && sync_fields(sim))
+	{
+		g->err = CPIC_ECUDA;
+		return -1;
+	}
+	return 0;
+}
+
+void
+stage_plasma_E(sim_t *sim)
+{
+	struct gpu_sim *g = GPU(sim);
+	int rc;
+	if(!g || g->err) return;
+	g->e_pending = 0;
+	if(!g->views_due) return;
+	double *e = g->ebuf;
+	for(int is = 0; is < (int) sim->nspecies; is++)
+	{
+		if((rc = cpic_gather_E(g->ctx, is, e, e + g->n[is])))
+		{
+			gpu_err("cpic_gather_E", rc);
+			g->err = rc;
+			return;
+		}
+		e += 2 * g->n[is];
+	}
+	g->e_pending = 1;
+}
+
+void
+stage_plasma_r(sim_t *sim)
+{
+	struct gpu_sim *g = GPU(sim);
+	int rc;
+	if(!g || g->err) return;
+	if((rc = cpic_stage_plasma(g->ctx)))
+	{
+		gpu_err("cpic_stage_plasma", rc);
+		g->err = rc;
+	}
+}
+
+void
+stage_field_rho(sim_t *sim)
+{
+	struct gpu_sim *g = GPU(sim);
+	if(!g || g->err) return;
+	if(g->views_due && (sync_fields(sim) || sync_particles(sim, g->e_pending ? g->ebuf : NULL)))
+		g->err = CPIC_ECUDA;
+	g->views_due = 0;
+	g->e_pending = 0;
+}
+
+int
+comm_plasma(sim_t *sim, int global_exchange)
+{
+	(void) global_exchange;
+	struct gpu_sim *g = GPU(sim);
+	return (!g || g->err) ? -1 : 0;
+}
+
+int
+particle_comm_initial(sim_t *sim)
+{
+	return comm_plasma(sim, 1);
+}
+
 int
 sim_step(sim_t *sim)
 {
 	struct gpu_sim *g = GPU(sim);
-	int rc, sync;
+	int rc;
 
-	if(sim->iter < 0 || !g) return -1;
+	if(sim->iter < 0 || !g || g->err) return -1;
 	if(sim->iter >= sim->cycles) return -1;
 
 	perf_reset(&sim->timers[TIMER_ITERATION]);
 	perf_start(&sim->timers[TIMER_ITERATION]);
 
-	sync = g->host_sync > 0 && (sim->iter % g->host_sync) == 0;
-	if(sync || sim->output->enabled)
+	if(views_due(sim, g) || sim->output->enabled)
 	{
-		/* split path: fields are needed on the host between the stages */
-		if((rc = cpic_stage_field_E(g->ctx))) { gpu_err("cpic_stage_field_E", rc); return -1; }
-		if(sim->output->enabled && (sync_fields(sim) || output_fields(sim)))
+		/* the reference's stage sequence (sim.c:509-565), with the host
+		 * views refreshed between the stages */
+		if(stage_field_E(sim))
 			return -1;
-		if(sync)
+		if(output_fields(sim))
 		{
-			/* E at the pre-push positions, as stage_plasma_E leaves it */
-			double *e = g->ebuf;
-			for(int is = 0; is < (int) sim->nspecies; is++)
-			{
-				if((rc = cpic_gather_E(g->ctx, is, e, e + g->n[is])))
-				{
-					gpu_err("cpic_gather_E", rc);
-					return -1;
-				}
-				e += 2 * g->n[is];
-			}
+			fprintf(stderr, "sim_gpu: output_fields failed\n");
+			return -1;
 		}
-		if((rc = cpic_stage_plasma(g->ctx))) { gpu_err("cpic_stage_plasma", rc); return -1; }
-		if(sync && (sync_fields(sim) || sync_particles(sim, g->ebuf)))
+		stage_plasma_E(sim);
+		stage_plasma_r(sim);
+		stage_field_rho(sim);
+		if(g->err)
 			return -1;
 	}
 	else if((rc = cpic_step(g->ctx)))
 	{
+		/* no host views this step: the whole step in one call */
 		gpu_err("cpic_step", rc);
+		g->err = rc;
 		return -1;
 	}
 

@@ -181,6 +181,14 @@ CPIC_API int cpic_selftest_wait(uint32_t polls);
 CPIC_API int cpic_time_steps(cpic_ctx_t *ctx, int64_t nsteps, double *ms_total,
 		double *ms_plasma, double *ms_field);
 
+/* No counterpart in the reference.  FP64 arithmetic peak of the current
+ * device, the denominator of the FP64 form's roofline: every thread of
+ * enough resident blocks runs independent chains of `iters` dependent FP64
+ * FMAs (2 FLOPs each), timed with CUDA events after one shorter warm-up
+ * launch.  gflops: measured GFLOP/s; ms (may be NULL): the timed launch.
+ * Changes no device setting. */
+CPIC_API int cpic_fp64_peak(int64_t iters, double *gflops, double *ms);
+
 /* Tile geometry chosen for this context: out[4] = {tile_x, tile_y, halo,
  * capacity slack in percent}. */
 CPIC_API int cpic_tile_info(const cpic_ctx_t *ctx, int32_t *out);

@@ -16,8 +16,21 @@ none of which exist here: mpi.h, fftw3*.h, nanos6/debug.h and hdf5.h come
 from oracle/shims, libconfig.h from include/ with this project's parser
 (cpic_gb300/csrc/cpic_conf.c).  The MFT_TAP backend (mft_tap.c, tap.c,
 mft_worker.c) and the plotter are left out; cpic.c is left out because the
-harness and the tests bring their own main.  x86-64 only (AVX2
-intrinsics).  The reference tree is read, never written.
+harness and the tests bring their own main.
+
+Hosts.  On x86-64 the reference's AVX2 code compiles with the system
+intrinsics headers (-march=core-avx2).  Elsewhere (the Arm host of the GPU)
+oracle/shims_portable/x86intrin.h stands in for them, lane by lane with the
+same IEEE semantics; on x86-64 the same portable build is made as a third
+variant (shipped_portable) that a CPU test checks bit for bit against the
+native one.
+
+Where the tree comes from (ref_root): the directory named by CPIC_REFERENCE
+(default /root/reference) when it exists; there stage() also lays out
+oracle/_ref/tree/ (git-ignored, never committed), the view of the tree's
+src/, include/, test/ and conf/ that the builds on the GPU host use, where
+the reference tree itself is absent.  The reference tree is read, never
+written.
 """
 import concurrent.futures as cf
 import os
@@ -29,10 +42,57 @@ REF = os.environ.get("CPIC_REFERENCE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_ref")
+TREE = os.path.join(OUT, "tree")
+STAGED_DIRS = ("src", "include", "test", "conf")
 SOURCES = ["sim", "field", "particle", "mover", "interpolate", "comm_plasma", "comm_field", "plist",
            "mat", "plasma", "specie", "config", "perf", "utils", "solver", "output", "boundary"]
-CFLAGS = ["-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-DNDEBUG", "-DUSE_VECTOR_256",
-          "-march=core-avx2", "-Wno-unknown-pragmas", "-w"]
+BASE_CFLAGS = ["-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-DNDEBUG", "-DUSE_VECTOR_256",
+               "-Wno-unknown-pragmas", "-w"]
+PORTABLE_INC = ["-I", os.path.join(HERE, "shims_portable")]
+
+
+def is_x86():
+    return platform.machine() in ("x86_64", "AMD64")
+
+
+def cflags(portable):
+    """Compiler flags of a reference build: native AVX2 on x86-64, else the
+    portable intrinsics (which go ahead of the system headers)."""
+    return BASE_CFLAGS + (PORTABLE_INC if portable else ["-march=core-avx2"])
+
+
+def stage():
+    """Lays out oracle/_ref/tree/ from the reference tree: one symlink per
+    file of its src/, include/, test/ and conf/ (data files included).
+    Returns the staged root, or None when the reference tree is absent."""
+    if not os.path.isdir(os.path.join(REF, "src")):
+        return None
+    for d in STAGED_DIRS:
+        src_d = os.path.join(REF, d)
+        if not os.path.isdir(src_d):
+            continue
+        for dirpath, _, files in os.walk(src_d):
+            rel = os.path.relpath(dirpath, REF)
+            dst_d = os.path.join(TREE, rel)
+            os.makedirs(dst_d, exist_ok=True)
+            for f in files:
+                dst = os.path.join(dst_d, f)
+                if os.path.lexists(dst):
+                    os.remove(dst)
+                os.symlink(os.path.join(dirpath, f), dst)
+    return TREE
+
+
+def ref_root():
+    """The reference tree to build from: CPIC_REFERENCE when present (after
+    refreshing the staged view), else the staged view if it holds the
+    sources, else None."""
+    if os.path.isdir(os.path.join(REF, "src")):
+        stage()
+        return REF
+    if os.path.isfile(os.path.join(TREE, "src", "sim.c")):
+        return TREE
+    return None
 
 
 def _run(cmd, cwd=None):
@@ -41,34 +101,40 @@ def _run(cmd, cwd=None):
         raise RuntimeError("%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
 
 
-def _farm(variant):
+def _farm(ref, variant):
     """Directory holding the variant's src view (symlinks only)."""
-    if variant == "shipped":
-        return os.path.join(REF, "src")
+    if variant != "exact":
+        return os.path.join(ref, "src")
     d = os.path.join(OUT, "exact_src")
     os.makedirs(d, exist_ok=True)
-    for f in os.listdir(os.path.join(REF, "src")):
+    for f in os.listdir(os.path.join(ref, "src")):
         if not (f.endswith(".c") or f.endswith(".h")):
             continue
         dst = os.path.join(d, f)
-        src = os.path.join(HERE, "exact", f) if f == "simd_avx2.h" else os.path.join(REF, "src", f)
-        if os.path.islink(dst) or os.path.exists(dst):
+        src = os.path.join(HERE, "exact", f) if f == "simd_avx2.h" else os.path.join(ref, "src", f)
+        if os.path.lexists(dst):
             os.remove(dst)
         os.symlink(src, dst)
     return d
 
 
+def variants():
+    """(name, portable) of the variants this host builds."""
+    if is_x86():
+        return [("shipped", False), ("exact", False), ("shipped_portable", True)]
+    return [("shipped", True), ("exact", True)]
+
+
 def build(force=False):
-    if not os.path.isdir(REF):
-        return None
-    if platform.machine() not in ("x86_64", "AMD64"):
+    ref = ref_root()
+    if ref is None:
         return None
     os.makedirs(OUT, exist_ok=True)
     stamp = os.path.join(OUT, "built.txt")
     if os.path.exists(stamp) and not force:
         return OUT
     inc = ["-I", os.path.join(HERE, "shims"), "-I", os.path.join(ROOT, "include"),
-           "-I", os.path.join(REF, "include")]
+           "-I", os.path.join(ref, "include")]
     jobs = []
     common_objs = []
     o = os.path.join(OUT, "shim_runtime.o")
@@ -80,20 +146,21 @@ def build(force=False):
                  "-o", o])
     common_objs.append(o)
     variant_objs = {}
-    for v in ("shipped", "exact"):
-        src = _farm(v)
-        extra = ['-DORC_REF_SIMD_AVX2="%s"' % os.path.join(REF, "src", "simd_avx2.h")] if v == "exact" else []
+    for v, portable in variants():
+        src = _farm(ref, v)
+        extra = ['-DORC_REF_SIMD_AVX2="%s"' % os.path.join(ref, "src", "simd_avx2.h")] if v == "exact" else []
+        flags = cflags(portable)
         vinc = ["-iquote", src] + inc
         objs = []
         for s in SOURCES:
             o = os.path.join(OUT, "%s_%s.o" % (v, s))
-            jobs.append(["gcc"] + CFLAGS + extra + vinc + ["-c", os.path.join(src, s + ".c"), "-o", o])
+            jobs.append(["gcc"] + flags + extra + vinc + ["-c", os.path.join(src, s + ".c"), "-o", o])
             objs.append(o)
         for name, path in (("harness", os.path.join(HERE, "ref_harness.c")),
-                           ("t_cs", os.path.join(REF, "test", "constant-speed.c")),
-                           ("t_cy", os.path.join(REF, "test", "cyclotron.c"))):
+                           ("t_cs", os.path.join(ref, "test", "constant-speed.c")),
+                           ("t_cy", os.path.join(ref, "test", "cyclotron.c"))):
             o = os.path.join(OUT, "%s_%s.o" % (v, name))
-            jobs.append(["gcc"] + CFLAGS + extra + ["-I", src] + inc + ["-c", path, "-o", o])
+            jobs.append(["gcc"] + flags + extra + ["-I", src] + inc + ["-c", path, "-o", o])
         variant_objs[v] = objs
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(_run, jobs))
@@ -103,7 +170,8 @@ def build(force=False):
             _run(["gcc", "-o", os.path.join(OUT, exe), os.path.join(OUT, "%s_%s.o" % (v, name))]
                  + objs + common_objs + ["-lm", "-lpthread"])
     with open(stamp, "w") as f:
-        f.write("reference built from %s/src with oracle shims\n" % REF)
+        f.write("reference built from %s/src with oracle shims (%s)\n"
+                % (ref, ", ".join(v for v, _ in variants())))
     return OUT
 
 

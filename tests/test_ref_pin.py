@@ -154,3 +154,24 @@ def test_harmonic_traces():
         ex = o.particle_E(0)[0][0]
         assert abs(x - r0[k]) <= 5e-7 * abs(r0[k]) + 1e-12, k
         assert abs(ex - e0[k]) <= 5e-7 * abs(e0[k]) + 1e-12, k
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(refrun.REF_OUT, "ref_harness_shipped_portable")),
+                    reason="the portable build is compared where the native AVX2 build exists")
+@pytest.mark.parametrize("which", ["two_stream", "two_species"])
+def test_portable_intrinsics_build_matches_native(which):
+    """The reference built with oracle/shims_portable/x86intrin.h (how it
+    builds on the Arm host of the GPU) gives the native AVX2 build's
+    results bit for bit: fields and every particle after the pre-step and
+    after steps 1-3, and the field energy of every step."""
+    case = cases.two_stream() if which == "two_stream" else cases.two_species(nx=32, ny=32, ppc=8)
+    steps = 50
+    a = refrun.run(case, steps, dumps=(1, 2, 3), variant="shipped")
+    b = refrun.run(case, steps, dumps=(1, 2, 3), variant="shipped_portable")
+    assert np.array_equal(a["energy"], b["energy"])
+    for k in ("pre", 1, 2, 3):
+        for f in ("rho", "phi", "Ex", "Ey"):
+            assert np.array_equal(a[k][f], b[k][f]), (k, f)
+        for sa, sb in zip(a[k]["species"], b[k]["species"]):
+            for f in ("order", "x", "y", "ux", "uy", "Ex", "Ey"):
+                assert np.array_equal(sa[f], sb[f]), (k, f)
