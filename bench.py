@@ -574,6 +574,14 @@ def study_phases(args):
                      "tile_max_over_mean": float(tc.max() / tc.mean()),
                      "tile_p99_over_mean": float(np.quantile(tc, 0.99) / tc.mean()),
                      "field_energy": ctx.field_energy()})
+    # the same state re-laid out with the initial 25 % slack: whether the
+    # late steps' cost comes from the store's spread (slack grown to 200 %)
+    before = ctx.layout_stats()
+    ctx.compact(25)
+    t = ctx.time_steps(blk)
+    rows.append({"step": done + blk, "after_compact_to_25pct": True, "slack_before": before["slack_pct"],
+                 "ms_step": t["ms_total"] / blk, "ms_push": t["ms_plasma"] / blk,
+                 "ms_field": t["ms_field"] / blk, "stats": ctx.layout_stats()})
     ctx.close()
     return {"study": "phases", "workload": desc, "tile": T, "rows": rows}
 
@@ -662,14 +670,14 @@ def ensemble_members(nruns, seed=2024):
             for i, (g, c, v, a) in enumerate(zip(grid, ppc, v0, amp))]
 
 
-def _member_ctx(m, precision, tile):
+def _member_ctx(m, precision, tile, ppt=0):
     from cpic_gb300 import _lib
     L = 2 * math.pi
     n = m["grid"] * m["grid"] * m["ppc"]
     x, y, ux, uy = _lib.init_two_stream(m["seed"], 0, n, L, L, m["v0"], 0.0, m["amp"])
     q = -L * L / n
     c = _lib.Context(m["grid"], m["grid"], L, L, 0.05, 1.0, (0.0, 0.0, 0.0), precision=precision,
-                     track_ids=False, tile=tile)
+                     track_ids=False, tile=tile, ppt=ppt)
     c.add_species(q, -q, x, y, ux, uy)
     c.pre_step()
     return c, n
@@ -739,16 +747,17 @@ def study_ensemble(args):
         key = (m["grid"], int(round(math.log2(m["ppc"]))))
         if key not in tiles:
             n = m["grid"] * m["grid"] * m["ppc"]
-            tiles[key] = _lib.autotune_tile(m["grid"], m["grid"], L, L, 0.05, n, m["v0"], 0.0)[0]
-        m["tile"] = tiles[key]
+            tiles[key] = _lib.autotune_layout(m["grid"], m["grid"], L, L, 0.05, n, m["v0"], 0.0)[:2]
+        m["tile"], m["ppt"] = tiles[key]
     t_tune = time.perf_counter() - t0
     res = {"study": "ensemble", "runs": len(members), "steps": steps, "precision": "mixed",
            "particles_total": int(sum(m["grid"] ** 2 * m["ppc"] for m in members)),
            "autotune_seconds": t_tune,
-           "autotuned_tiles": {"%dx%d ppc~2^%d" % (k[0], k[0], k[1]): v for k, v in sorted(tiles.items())}}
+           "autotuned_layouts": {"%dx%d ppc~2^%d" % (k[0], k[0], k[1]): {"tile": v[0], "ppt": v[1]}
+                                 for k, v in sorted(tiles.items())}}
     pstep = res["particles_total"] * steps
     # one graph for all runs
-    runs = [_member_ctx(m, _lib.MIXED, m["tile"])[0] for m in members]
+    runs = [_member_ctx(m, _lib.MIXED, m["tile"], m["ppt"])[0] for m in members]
     ens = _lib.Ensemble(runs)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -764,7 +773,7 @@ def study_ensemble(args):
     # the same runs one after another, no graph
     t_seq = 0.0
     for m in members:
-        c, n = _member_ctx(m, _lib.MIXED, m["tile"])
+        c, n = _member_ctx(m, _lib.MIXED, m["tile"], m["ppt"])
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         c.run(steps)
@@ -778,7 +787,7 @@ def study_ensemble(args):
         lin = min(300, steps)
         errs = []
         for m in members:
-            cm, _ = _member_ctx(m, _lib.MIXED, m["tile"])
+            cm, _ = _member_ctx(m, _lib.MIXED, m["tile"], m["ppt"])
             cf, _ = _member_ctx(m, _lib.FP64, 0)
             worst = 0.0
             for k in range(0, lin, 20):

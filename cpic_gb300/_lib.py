@@ -35,7 +35,7 @@ class Params(ctypes.Structure):
         ("plasma_chunks", ctypes.c_int64), ("cycles", ctypes.c_int64),
         ("precision", ctypes.c_int32), ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32),
         ("halo", ctypes.c_int32), ("track_ids", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("particles_per_thread", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -79,6 +79,7 @@ SIGNATURES = [
     ("cpic_diag", ctypes.c_int, [ctypes.c_void_p, D]),
     ("cpic_field_energy", ctypes.c_int, [ctypes.c_void_p, D]),
     ("cpic_selftest_wait", ctypes.c_int, [ctypes.c_uint32]),
+    ("cpic_compact", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("cpic_fp64_peak", ctypes.c_int, [ctypes.c_int64, D, D]),
     ("cpic_status_bits", ctypes.c_uint32, [ctypes.c_void_p]),
     ("cpic_time_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, D, D, D]),
@@ -93,6 +94,9 @@ SIGNATURES = [
                                          ctypes.POINTER(ctypes.c_int32)]),
     ("cpic_autotune_tile", ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, ctypes.c_double,
                                           ctypes.c_double, ctypes.POINTER(ctypes.c_int32), D]),
+    ("cpic_autotune_layout", ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, ctypes.c_double,
+                                            ctypes.c_double, ctypes.POINTER(ctypes.c_int32),
+                                            ctypes.POINTER(ctypes.c_int32), D]),
     ("cpic_adj_create", ctypes.c_int, [ctypes.POINTER(AdjParams), ctypes.c_int64,
                                        ctypes.POINTER(ctypes.c_void_p)]),
     ("cpic_adj_destroy", None, [ctypes.c_void_p]),
@@ -160,7 +164,7 @@ class Context:
     """One resident simulation (cpic_ctx_t)."""
 
     def __init__(self, nx, ny, Lx, Ly, dt, e0=1.0, B=(0.0, 0.0, 0.0), precision=FP64,
-                 plasma_chunks=1, cycles=0, tile=0, halo=0, track_ids=True):
+                 plasma_chunks=1, cycles=0, tile=0, halo=0, track_ids=True, ppt=0):
         self.lib = load()
         p = Params()
         p.nx, p.ny, p.Lx, p.Ly, p.dt, p.e0 = nx, ny, Lx, Ly, dt, e0
@@ -168,6 +172,7 @@ class Context:
         p.plasma_chunks, p.cycles = plasma_chunks, cycles
         p.precision, p.tile_x, p.tile_y, p.halo = precision, tile, tile, halo
         p.track_ids = 1 if track_ids else 0
+        p.particles_per_thread = ppt
         h = ctypes.c_void_p()
         self._check(self.lib.cpic_create(ctypes.byref(p), ctypes.byref(h)), "cpic_create")
         self.h = h
@@ -267,6 +272,9 @@ class Context:
         out = np.empty(5)
         self._check(self.lib.cpic_diag(self.h, _dp(out)), "cpic_diag")
         return dict(WE=out[0], KE=out[1], Q=out[2], Px=out[3], Py=out[4])
+
+    def compact(self, slack_pct):
+        self._check(self.lib.cpic_compact(self.h, slack_pct), "cpic_compact")
 
     def field_energy(self):
         out = np.empty(2)
@@ -387,6 +395,22 @@ def autotune_tile(nx, ny, Lx, Ly, dt, n, v0, vth, precision=MIXED, e0=1.0):
     if r < 0:
         raise CpicError(r, "cpic_autotune_tile")
     return t.value, ms.value
+
+
+def autotune_layout(nx, ny, Lx, Ly, dt, n, v0, vth, precision=MIXED, e0=1.0):
+    """(tile, particles per thread, ms per step) chosen by the library's
+    autotuner over both."""
+    lib = load()
+    p = Params()
+    p.nx, p.ny, p.Lx, p.Ly, p.dt, p.e0 = nx, ny, Lx, Ly, dt, e0
+    p.plasma_chunks, p.precision = 1, precision
+    t, ppt = ctypes.c_int32(), ctypes.c_int32()
+    ms = ctypes.c_double()
+    r = lib.cpic_autotune_layout(ctypes.byref(p), n, v0, vth, ctypes.byref(t), ctypes.byref(ppt),
+                                 ctypes.byref(ms))
+    if r < 0:
+        raise CpicError(r, "cpic_autotune_layout")
+    return t.value, ppt.value, ms.value
 
 
 def fp64_peak(iters=1 << 16):

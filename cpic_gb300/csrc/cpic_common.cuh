@@ -33,16 +33,28 @@ constexpr int kMaxSpecies = 8;
 #ifndef CPIC_PPT
 #define CPIC_PPT 2
 #endif
+// Chunks of a tile requested into L2 ahead of the one being staged into
+// shared memory (0: none), so that more of the tile is in flight than the
+// two shared-memory buffers hold.
+#ifndef CPIC_PREFETCH_CHUNKS
+#define CPIC_PREFETCH_CHUNKS 2
+#endif
 constexpr int kPushThreads = CPIC_PUSH_THREADS;
-constexpr int kPPT = CPIC_PPT;                // particles per thread per chunk
-constexpr int kChunk = kPushThreads * kPPT;   // particles per chunk
+constexpr int kPrefetchChunks = CPIC_PREFETCH_CHUNKS;
+// Particles per thread per chunk: the default, and the compiled instances of
+// the fused kernel a context may choose from (the autotuner times them).
+constexpr int kPPT = CPIC_PPT;
+constexpr int kPPTChoices[] = {1, 2, 4};
 constexpr int kWeightBits = 18;
+// Particles per chunk with P particles per thread.
+__host__ __device__ constexpr int chunk_of(int P) { return kPushThreads * P; }
 // 32-bit shared weight sums: a node gains at most 2^kWeightBits per
-// particle, so kCheckChunks chunks add at most 2^30 to any node; a check
-// every kCheckChunks chunks that finds every node below 2^30 keeps every
+// particle, so check_chunks(P) chunks add at most 2^30 to any node; a check
+// every check_chunks(P) chunks that finds every node below 2^30 keeps every
 // sum below 2^31 until the next check
-constexpr int kCheckChunks = (1 << (30 - kWeightBits)) / kChunk;
-static_assert(kCheckChunks >= 1, "chunk too large for 32-bit weight sums");
+__host__ __device__ constexpr int check_chunks(int P) { return (1 << (30 - kWeightBits)) / chunk_of(P); }
+static_assert(check_chunks(4) >= 1, "chunk too large for 32-bit weight sums");
+inline bool ppt_supported(int P) { return P == 1 || P == 2 || P == 4; }
 
 // Device status bits (sticky until the host clears them).
 enum : uint32_t {
@@ -315,6 +327,14 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 			:: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
+// Hint to bring [src, src + bytes) of global memory into L2 (src 16-byte
+// aligned, bytes a multiple of 16).  Nothing waits for it; a later bulk copy
+// of the same bytes then reads from L2.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes)
+{
+	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
 	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(bar)) : "memory");
@@ -421,8 +441,9 @@ inline cudaError_t set_max_dyn_smem(std::initializer_list<const void *> fns, int
 // return cudaError_t report a failed one-time kernel set-up; launch errors
 // are left for the caller's cudaGetLastError.
 namespace cpic {
-cudaError_t launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
-int push_f64_blocks_per_sm(size_t smem);
+// ppt: particles per thread of the fused kernel's instance (kPPTChoices)
+cudaError_t launch_push_f64(const PushArgs &a, int ntiles, size_t smem, int ppt, cudaStream_t s);
+int push_f64_blocks_per_sm(size_t smem, int ppt);
 void launch_spill_f64(const SpillArgs &a, cudaStream_t s);
 void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s);
 cudaError_t launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
@@ -430,10 +451,10 @@ cudaError_t launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 		const double *cosy, double *phi, cudaStream_t s, const long long *rho_lo, double qinv_lo,
 		const double *Gt);
 
-cudaError_t launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s);
+cudaError_t launch_push_mix(const PushArgs &a, int ntiles, size_t smem, int ppt, cudaStream_t s);
 // resident blocks per SM of the mixed fused kernel at this dynamic shared
 // memory, for a store with or without ids (0 on error)
-int push_mix_blocks_per_sm(size_t smem, bool ids);
+int push_mix_blocks_per_sm(size_t smem, bool ids, int ppt);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
 cudaError_t launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,

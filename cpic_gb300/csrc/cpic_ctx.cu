@@ -50,6 +50,7 @@ struct cpic_ctx {
 	cpic_params_t p;
 	Grid g;
 	int ntiles;
+	int ppt;                  // particles per thread of the fused kernel's instance
 	int precision;
 	int64_t iter;
 	bool prepared;
@@ -815,9 +816,10 @@ static size_t push_smem_h(const cpic_ctx *c, int halo)
 	// two staged chunks plus the form's accumulators and field tile
 	int W = c->g.tx + 2 * halo + 1;
 	// (+128: the kernel rounds the dynamic base up to 128 bytes)
+	const int C = chunk_of(c->ppt);
 	if(c->precision == CPIC_MIXED)
-		return 128 + 2 * Mix::stage_bytes(c->p.track_ids != 0) + Mix::smem_bytes(W, c->g.tx);
-	return 128 + 2 * F64::stage_bytes(true) + F64::smem_bytes(W, c->g.tx);
+		return 128 + 2 * Mix::stage_bytes(c->p.track_ids != 0, C) + Mix::smem_bytes(W, c->g.tx);
+	return 128 + 2 * F64::stage_bytes(true, C) + F64::smem_bytes(W, c->g.tx);
 }
 
 static size_t push_smem(const cpic_ctx *c)
@@ -966,14 +968,11 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	int32_t *key1 = nullptr, *key2 = nullptr;
 	if(blk)
 	{
-		static bool attr = false;
-		if(!attr)
-		{
-			const int mx = 2 * kBlkSortMaxTiles * (int) sizeof(int32_t);
-			cudaFuncSetAttribute(k_rb_convert<Mix>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			cudaFuncSetAttribute(k_rb_convert<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-			attr = true;
-		}
+		static PerDeviceOnce once;
+		CK(once.run([] {
+			return set_max_dyn_smem({(const void *) k_rb_convert<Mix>, (const void *) k_rb_convert<F64>},
+					2 * kBlkSortMaxTiles * (int) sizeof(int32_t));
+		}));
 		int r = alloc_store(c, tmp1, nstage, false);
 		if(r) return r;
 		CK(cudaMalloc(&key1, nstage * sizeof(int32_t)));
@@ -1171,7 +1170,8 @@ static bool tile_order_pays(const cpic_ctx *c, size_t smem)
 			|| cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
 		return true;
 	const int per_sm = c->precision == CPIC_MIXED
-		? push_mix_blocks_per_sm(smem, c->p.track_ids != 0) : push_f64_blocks_per_sm(smem);
+		? push_mix_blocks_per_sm(smem, c->p.track_ids != 0, c->ppt)
+		: push_f64_blocks_per_sm(smem, c->ppt);
 	return per_sm <= 0 || (int64_t) c->ntiles > (int64_t) per_sm * nsm;
 }
 
@@ -1216,9 +1216,9 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 		launch_spill_f64(sa, st);
 	if(ev0) CK(cudaEventRecord(ev0, st));
 	if(c->precision == CPIC_MIXED)
-		CK(launch_push_mix(sa.p, c->ntiles, smem, st));
+		CK(launch_push_mix(sa.p, c->ntiles, smem, c->ppt, st));
 	else
-		CK(launch_push_f64(sa.p, c->ntiles, smem, st));
+		CK(launch_push_f64(sa.p, c->ntiles, smem, c->ppt, st));
 	if(ev1) CK(cudaEventRecord(ev1, st));
 	CK(cudaGetLastError());
 	// the tile fix-up: bandwidth-bound, so with `overlap` it runs on the
@@ -1349,6 +1349,12 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	}
 	int TY = p->tile_y > 0 ? p->tile_y : T;
 	if(!pow2(T) || !pow2(TY) || p->nx % T || p->ny % TY || T != TY)
+	{
+		delete c;
+		return CPIC_EINVAL;
+	}
+	c->ppt = p->particles_per_thread > 0 ? p->particles_per_thread : kPPT;
+	if(!ppt_supported(c->ppt))
 	{
 		delete c;
 		return CPIC_EINVAL;
@@ -1628,8 +1634,9 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 		int H = std::max(hmin, std::min((int) ceil(1.2 * D) + 1, c->g.tx));
 		if(c->precision == CPIC_MIXED)
 		{
-			int target = push_mix_blocks_per_sm(push_smem_h(c, hmin), c->p.track_ids != 0);
-			while(H > hmin && push_mix_blocks_per_sm(push_smem_h(c, H), c->p.track_ids != 0) < target)
+			int target = push_mix_blocks_per_sm(push_smem_h(c, hmin), c->p.track_ids != 0, c->ppt);
+			while(H > hmin && push_mix_blocks_per_sm(push_smem_h(c, H), c->p.track_ids != 0, c->ppt)
+					< target)
 				H--;
 		}
 		c->g.halo = H;
@@ -1976,6 +1983,23 @@ CPIC_API uint32_t cpic_status_bits(cpic_ctx_t *c)
 	return st;
 }
 
+// Re-lays the particle store out with the given capacity slack (a
+// counting-sort rebuild from the current tiles and spill list).
+CPIC_API int cpic_compact(cpic_ctx_t *c, int32_t slack_pct)
+{
+	if(!c || slack_pct < 0 || slack_pct > 1000) return CPIC_EINVAL;
+	if(!c->prepared) return CPIC_ESTATE;
+	int r = join_fixup(c);
+	if(r) return r;
+	CK(cudaStreamSynchronize(c->stream));
+	c->slack_pct = slack_pct;
+	for(int s = 0; s < c->nspecies; s++)
+		if((r = rebuild_species(c, s, false, nullptr, 0)))
+			return r;
+	CK(cudaStreamSynchronize(c->stream));
+	return check_status(c);
+}
+
 // One warp waits on an mbarrier phase that cannot complete: thread 0 arms it
 // for 16 bytes of a bulk copy that is never issued, so no copy is in flight
 // and the wait can only expire.  The status word records ST_TIMEOUT.
@@ -2076,9 +2100,9 @@ CPIC_API int cpic_layout_stats(const cpic_ctx_t *c, int64_t *out)
 	if(c->nspecies > 0)
 	{
 		if(c->precision == CPIC_MIXED)
-			out[3] = push_mix_blocks_per_sm(push_smem(c), c->p.track_ids != 0);
+			out[3] = push_mix_blocks_per_sm(push_smem(c), c->p.track_ids != 0, c->ppt);
 		else
-			out[3] = push_f64_blocks_per_sm(push_smem(c));
+			out[3] = push_f64_blocks_per_sm(push_smem(c), c->ppt);
 	}
 	return CPIC_OK;
 }
@@ -2385,21 +2409,28 @@ CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_gr
 // particle count: each candidate runs a seeded two-stream plasma of n
 // particles for 3 + 6 steps, the fastest by CUDA events wins.  Results are
 // kept per (grid, log2 particles per cell, precision) for the process.
-CPIC_API int cpic_autotune_tile(const cpic_params_t *p, int64_t n, double v0, double vth,
-		int32_t *tile, double *ms_per_step)
+// Times a seeded two-stream plasma (beam speed v0, spread vth, amplitude
+// 0.01) with every tile size, and with every particles-per-thread instance
+// when tune_ppt (else the context's own choice, p->particles_per_thread);
+// the fastest layout wins.  Cached per (grid, log2 particles per cell,
+// precision, what was tuned) for the process.
+static int autotune(const cpic_params_t *p, int64_t n, double v0, double vth, bool tune_ppt,
+		int32_t *tile, int32_t *ppt, double *ms_per_step)
 {
-	if(!p || n <= 0 || !tile) return CPIC_EINVAL;
-	struct Key { int64_t nx, ny; int lppc, prec; double ms; int32_t T; };
+	struct Key { int64_t nx, ny; int lppc, prec, tp, fixed_ppt; double ms; int32_t T, P; };
 	static std::vector<Key> cache;
 	static std::mutex mu;
 	double ppc = (double) n / ((double) p->nx * (double) p->ny);
 	int lppc = (int) lround(log2(ppc > 0 ? ppc : 1.0));
+	int fixed = tune_ppt ? 0 : p->particles_per_thread;
 	{
 		std::lock_guard<std::mutex> lk(mu);
 		for(const Key &k : cache)
-			if(k.nx == p->nx && k.ny == p->ny && k.lppc == lppc && k.prec == p->precision)
+			if(k.nx == p->nx && k.ny == p->ny && k.lppc == lppc && k.prec == p->precision
+					&& k.tp == (int) tune_ppt && k.fixed_ppt == fixed)
 			{
 				*tile = k.T;
+				if(ppt) *ppt = k.P;
 				if(ms_per_step) *ms_per_step = k.ms;
 				return CPIC_OK;
 			}
@@ -2408,36 +2439,57 @@ CPIC_API int cpic_autotune_tile(const cpic_params_t *p, int64_t n, double v0, do
 	cpic_init_two_stream(1, 0, n, p->Lx, p->Ly, v0, vth, 0.01, x.data(), y.data(), ux.data(),
 			uy.data());
 	double q = -p->Lx * p->Ly / (double) n;
-	int32_t best = 0;
+	int32_t best = 0, best_p = 0;
 	double best_ms = INFINITY;
 	for(int32_t T = 4; T <= 64; T *= 2)
 	{
 		if(p->nx % T || p->ny % T || (p->nx / T) * (p->ny / T) < 4) continue;
-		cpic_params_t q2 = *p;
-		q2.tile_x = q2.tile_y = T;
-		q2.cycles = 0;
-		cpic_ctx_t *c = nullptr;
-		int r = cpic_create(&q2, &c);
-		if(r) continue;
-		double ms = INFINITY;
-		if(cpic_add_species(c, q, -q, n, x.data(), y.data(), ux.data(), uy.data()) >= 0
-				&& cpic_pre_step(c) == CPIC_OK && cpic_step(c) == CPIC_OK
-				&& cpic_time_steps(c, 3, nullptr, nullptr, nullptr) == CPIC_OK)
+		for(int P : kPPTChoices)
 		{
-			double tot = 0.0;
-			if(cpic_time_steps(c, 6, &tot, nullptr, nullptr) == CPIC_OK) ms = tot / 6.0;
+			if(!tune_ppt && P != (fixed > 0 ? fixed : kPPT)) continue;
+			cpic_params_t q2 = *p;
+			q2.tile_x = q2.tile_y = T;
+			q2.particles_per_thread = P;
+			q2.cycles = 0;
+			cpic_ctx_t *c = nullptr;
+			int r = cpic_create(&q2, &c);
+			if(r) continue;
+			double ms = INFINITY;
+			if(cpic_add_species(c, q, -q, n, x.data(), y.data(), ux.data(), uy.data()) >= 0
+					&& cpic_pre_step(c) == CPIC_OK && cpic_step(c) == CPIC_OK
+					&& cpic_time_steps(c, 3, nullptr, nullptr, nullptr) == CPIC_OK)
+			{
+				double tot = 0.0;
+				if(cpic_time_steps(c, 6, &tot, nullptr, nullptr) == CPIC_OK) ms = tot / 6.0;
+			}
+			cpic_destroy(c);
+			if(ms < best_ms) { best_ms = ms; best = T; best_p = P; }
 		}
-		cpic_destroy(c);
-		if(ms < best_ms) { best_ms = ms; best = T; }
 	}
 	if(!best) return CPIC_EINVAL;
 	{
 		std::lock_guard<std::mutex> lk(mu);
-		cache.push_back(Key{p->nx, p->ny, lppc, p->precision, best_ms, best});
+		cache.push_back(Key{p->nx, p->ny, lppc, p->precision, (int) tune_ppt, fixed, best_ms, best,
+				best_p});
 	}
 	*tile = best;
+	if(ppt) *ppt = best_p;
 	if(ms_per_step) *ms_per_step = best_ms;
 	return CPIC_OK;
+}
+
+CPIC_API int cpic_autotune_tile(const cpic_params_t *p, int64_t n, double v0, double vth,
+		int32_t *tile, double *ms_per_step)
+{
+	if(!p || n <= 0 || !tile) return CPIC_EINVAL;
+	return autotune(p, n, v0, vth, false, tile, nullptr, ms_per_step);
+}
+
+CPIC_API int cpic_autotune_layout(const cpic_params_t *p, int64_t n, double v0, double vth,
+		int32_t *tile, int32_t *particles_per_thread, double *ms_per_step)
+{
+	if(!p || n <= 0 || !tile || !particles_per_thread) return CPIC_EINVAL;
+	return autotune(p, n, v0, vth, true, tile, particles_per_thread, ms_per_step);
 }
 
 } // extern "C"

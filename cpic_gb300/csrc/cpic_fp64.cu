@@ -70,30 +70,47 @@ void launch_gather_f64_tiles(const Grid &g, const StoreF64 &st, const int64_t *b
 
 static PerDeviceOnce g_push_f64_once, g_poisson_f64_once;
 
+// The fused kernel's instance for P particles per thread.
+static const void *push_f64_fn(int P)
+{
+	switch(P)
+	{
+		case 1: return (const void *) k_push<F64, F64::kMinBlocks, true, 1>;
+		case 4: return (const void *) k_push<F64, F64::kMinBlocks, true, 4>;
+		default: return (const void *) k_push<F64, F64::kMinBlocks, true, 2>;
+	}
+}
+
 static cudaError_t push_f64_attrs()
 {
 	return g_push_f64_once.run([] {
-		return set_max_dyn_smem({(const void *) k_push<F64>}, 200 * 1024, true);
+		return set_max_dyn_smem({push_f64_fn(1), push_f64_fn(2), push_f64_fn(4)}, 200 * 1024, true);
 	});
 }
 
-int push_f64_blocks_per_sm(size_t smem)
+int push_f64_blocks_per_sm(size_t smem, int ppt)
 {
-	if(push_f64_attrs() != cudaSuccess)
+	if(!ppt_supported(ppt) || push_f64_attrs() != cudaSuccess)
 		return 0;
 	int b = 0;
-	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_push<F64>, kPushThreads, smem)
+	if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, push_f64_fn(ppt), kPushThreads, smem)
 			!= cudaSuccess)
 		return 0;
 	return b;
 }
 
-cudaError_t launch_push_f64(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+cudaError_t launch_push_f64(const PushArgs &a, int ntiles, size_t smem, int ppt, cudaStream_t s)
 {
+	if(!ppt_supported(ppt)) return cudaErrorInvalidValue;
 	cudaError_t e = push_f64_attrs();
 	if(e != cudaSuccess) return e;
 	for(int sp = 0; sp < a.nspecies; sp++)
-		k_push<F64><<<ntiles, kPushThreads, smem, s>>>(species_args(a, sp));
+	{
+		const PushArgs b = species_args(a, sp);
+		if(ppt == 1) k_push<F64, F64::kMinBlocks, true, 1><<<ntiles, kPushThreads, smem, s>>>(b);
+		else if(ppt == 4) k_push<F64, F64::kMinBlocks, true, 4><<<ntiles, kPushThreads, smem, s>>>(b);
+		else k_push<F64, F64::kMinBlocks, true, 2><<<ntiles, kPushThreads, smem, s>>>(b);
+	}
 	return cudaSuccess;
 }
 

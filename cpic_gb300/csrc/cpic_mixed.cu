@@ -81,13 +81,33 @@ void launch_gather_mix_tiles(const Grid &g, const StoreMix &st, const int64_t *b
 
 static PerDeviceOnce g_push_mix_once, g_poisson_mix_once;
 
+// The fused kernel's instance: register-capped (Mix::kHiBlocks resident
+// blocks) or not, store with or without ids, P particles per thread.
+template <int P>
+static const void *push_mix_fn_p(bool hi, bool ids)
+{
+	if(hi)
+		return ids ? (const void *) k_push<Mix, Mix::kHiBlocks, true, P>
+			: (const void *) k_push<Mix, Mix::kHiBlocks, false, P>;
+	return ids ? (const void *) k_push<Mix, Mix::kMinBlocks, true, P>
+		: (const void *) k_push<Mix, Mix::kMinBlocks, false, P>;
+}
+
+static const void *push_mix_fn(bool hi, bool ids, int P)
+{
+	return P == 1 ? push_mix_fn_p<1>(hi, ids) : P == 4 ? push_mix_fn_p<4>(hi, ids)
+		: push_mix_fn_p<2>(hi, ids);
+}
+
 static cudaError_t push_mix_attrs()
 {
 	return g_push_mix_once.run([] {
-		return set_max_dyn_smem({(const void *) k_push<Mix, Mix::kMinBlocks, false>,
-				(const void *) k_push<Mix, Mix::kHiBlocks, false>,
-				(const void *) k_push<Mix, Mix::kMinBlocks, true>,
-				(const void *) k_push<Mix, Mix::kHiBlocks, true>}, 200 * 1024, true);
+		cudaError_t e = cudaSuccess;
+		for(int P : kPPTChoices)
+			for(int hi = 0; hi < 2 && e == cudaSuccess; hi++)
+				for(int ids = 0; ids < 2 && e == cudaSuccess; ids++)
+					e = set_max_dyn_smem({push_mix_fn(hi != 0, ids != 0, P)}, 200 * 1024, true);
+		return e;
 	});
 }
 
@@ -95,51 +115,57 @@ static cudaError_t push_mix_attrs()
 // Mix::kHiBlocks resident blocks per SM with this much dynamic shared
 // memory (else the unconstrained instance runs).  The ids and no-ids
 // instances of a block count use the same registers within a few.
-static bool push_mix_hi(size_t smem, bool ids)
+static bool push_mix_hi(size_t smem, bool ids, int ppt)
 {
 	if(push_mix_attrs() != cudaSuccess)
 		return false;
 	int hi = 0;
-	cudaError_t e = ids
-		? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, k_push<Mix, Mix::kHiBlocks, true>,
-				kPushThreads, smem)
-		: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, k_push<Mix, Mix::kHiBlocks, false>,
-				kPushThreads, smem);
+	cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hi, push_mix_fn(true, ids, ppt),
+			kPushThreads, smem);
 	return e == cudaSuccess && hi >= Mix::kHiBlocks;
 }
 
-int push_mix_blocks_per_sm(size_t smem, bool ids)
+int push_mix_blocks_per_sm(size_t smem, bool ids, int ppt)
 {
-	if(push_mix_hi(smem, ids))
+	if(!ppt_supported(ppt))
+		return 0;
+	if(push_mix_hi(smem, ids, ppt))
 		return Mix::kHiBlocks;
 	int lo = 0;
-	cudaError_t e = ids
-		? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, k_push<Mix, Mix::kMinBlocks, true>,
-				kPushThreads, smem)
-		: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, k_push<Mix, Mix::kMinBlocks, false>,
-				kPushThreads, smem);
+	cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, push_mix_fn(false, ids, ppt),
+			kPushThreads, smem);
 	return e == cudaSuccess ? lo : 0;
 }
 
-cudaError_t launch_push_mix(const PushArgs &a, int ntiles, size_t smem, cudaStream_t s)
+template <int P>
+static void launch_push_mix_p(const PushArgs &b, int ntiles, size_t smem, bool hi, bool ids,
+		cudaStream_t s)
 {
+	if(ids)
+	{
+		if(hi) k_push<Mix, Mix::kHiBlocks, true, P><<<ntiles, kPushThreads, smem, s>>>(b);
+		else k_push<Mix, Mix::kMinBlocks, true, P><<<ntiles, kPushThreads, smem, s>>>(b);
+	}
+	else
+	{
+		if(hi) k_push<Mix, Mix::kHiBlocks, false, P><<<ntiles, kPushThreads, smem, s>>>(b);
+		else k_push<Mix, Mix::kMinBlocks, false, P><<<ntiles, kPushThreads, smem, s>>>(b);
+	}
+}
+
+cudaError_t launch_push_mix(const PushArgs &a, int ntiles, size_t smem, int ppt, cudaStream_t s)
+{
+	if(!ppt_supported(ppt)) return cudaErrorInvalidValue;
 	cudaError_t e = push_mix_attrs();
 	if(e != cudaSuccess) return e;
 	for(int sp = 0; sp < a.nspecies; sp++)
 	{
 		const PushArgs b = species_args(a, sp);
 		const bool ids = b.mix[0].id != nullptr;
-		const bool hi = push_mix_hi(smem, ids);
-		if(ids)
-		{
-			if(hi) k_push<Mix, Mix::kHiBlocks, true><<<ntiles, kPushThreads, smem, s>>>(b);
-			else k_push<Mix, Mix::kMinBlocks, true><<<ntiles, kPushThreads, smem, s>>>(b);
-		}
-		else
-		{
-			if(hi) k_push<Mix, Mix::kHiBlocks, false><<<ntiles, kPushThreads, smem, s>>>(b);
-			else k_push<Mix, Mix::kMinBlocks, false><<<ntiles, kPushThreads, smem, s>>>(b);
-		}
+		const bool hi = push_mix_hi(smem, ids, ppt);
+		if(ppt == 1) launch_push_mix_p<1>(b, ntiles, smem, hi, ids, s);
+		else if(ppt == 4) launch_push_mix_p<4>(b, ntiles, smem, hi, ids, s);
+		else launch_push_mix_p<2>(b, ntiles, smem, hi, ids, s);
 	}
 	return cudaSuccess;
 }

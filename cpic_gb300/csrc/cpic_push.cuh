@@ -73,13 +73,15 @@ struct F64 {
 		store(a, s, i, r);
 	}
 
-	// Staged chunk layout: x, y, ux, uy (kChunk doubles each), id.
-	static __host__ __device__ __forceinline__ size_t stage_bytes(bool)
+	// Staged chunk layout: x, y, ux, uy (C doubles each), id, for a chunk
+	// of C particles.
+	static __host__ __device__ __forceinline__ size_t stage_bytes(bool, int C)
 	{
-		return (size_t) kChunk * (4 * sizeof(double) + sizeof(int32_t));
+		return (size_t) C * (4 * sizeof(double) + sizeof(int32_t));
 	}
 
 	// Thread 0: arm `bar` and copy particles [c0, c0 + cnt) of the tile.
+	template <int C>
 	static __device__ __forceinline__ void stage_issue(const PushArgs &a, int s, int64_t first,
 			int cnt, unsigned char *buf, uint64_t *bar)
 	{
@@ -88,18 +90,33 @@ struct F64 {
 		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
 		mbar_arrive_expect_tx(bar, 4 * b8 + b4);
 		bulk_g2s(buf, st.x + first, b8, bar);
-		bulk_g2s(buf + kChunk * 8, st.y + first, b8, bar);
-		bulk_g2s(buf + kChunk * 16, st.ux + first, b8, bar);
-		bulk_g2s(buf + kChunk * 24, st.uy + first, b8, bar);
-		bulk_g2s(buf + kChunk * 32, st.id + first, b4, bar);
+		bulk_g2s(buf + C * 8, st.y + first, b8, bar);
+		bulk_g2s(buf + C * 16, st.ux + first, b8, bar);
+		bulk_g2s(buf + C * 24, st.uy + first, b8, bar);
+		bulk_g2s(buf + C * 32, st.id + first, b4, bar);
 	}
 
+	// L2 prefetch of the particles [first, first + cnt) of the tile.
+	static __device__ __forceinline__ void stage_prefetch(const PushArgs &a, int s, int64_t first,
+			int cnt)
+	{
+		const StoreF64 &st = a.f64[s];
+		uint32_t b8 = (uint32_t) ((cnt * 8 + 15) & ~15);
+		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
+		bulk_prefetch_l2(st.x + first, b8);
+		bulk_prefetch_l2(st.y + first, b8);
+		bulk_prefetch_l2(st.ux + first, b8);
+		bulk_prefetch_l2(st.uy + first, b8);
+		bulk_prefetch_l2(st.id + first, b4);
+	}
+
+	template <int C>
 	static __device__ __forceinline__ Rec from_stage(const unsigned char *buf, int j, bool)
 	{
 		const double *d = reinterpret_cast<const double *>(buf);
 		Rec r;
-		r.x = d[j]; r.y = d[kChunk + j]; r.ux = d[2 * kChunk + j]; r.uy = d[3 * kChunk + j];
-		r.id = reinterpret_cast<const int32_t *>(buf + kChunk * 32)[j];
+		r.x = d[j]; r.y = d[C + j]; r.ux = d[2 * C + j]; r.uy = d[3 * C + j];
+		r.id = reinterpret_cast<const int32_t *>(buf + C * 32)[j];
 		return r;
 	}
 
@@ -409,13 +426,14 @@ struct Mix {
 		if(kIds) st.id[i] = r.id;
 	}
 
-	// Staged chunk layout: cell, ox, oy, ux, uy (kChunk 32-bit words
-	// each) and, when ids are tracked, id.
-	static __host__ __device__ __forceinline__ size_t stage_bytes(bool ids)
+	// Staged chunk layout: cell, ox, oy, ux, uy (C 32-bit words each)
+	// and, when ids are tracked, id, for a chunk of C particles.
+	static __host__ __device__ __forceinline__ size_t stage_bytes(bool ids, int C)
 	{
-		return (size_t) kChunk * 4 * (ids ? 6 : 5);
+		return (size_t) C * 4 * (ids ? 6 : 5);
 	}
 
+	template <int C>
 	static __device__ __forceinline__ void stage_issue(const PushArgs &a, int s, int64_t first,
 			int cnt, unsigned char *buf, uint64_t *bar)
 	{
@@ -423,22 +441,38 @@ struct Mix {
 		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
 		mbar_arrive_expect_tx(bar, (st.id ? 6 : 5) * b4);
 		bulk_g2s(buf, st.cell + first, b4, bar);
-		bulk_g2s(buf + kChunk * 4, st.ox + first, b4, bar);
-		bulk_g2s(buf + kChunk * 8, st.oy + first, b4, bar);
-		bulk_g2s(buf + kChunk * 12, st.ux + first, b4, bar);
-		bulk_g2s(buf + kChunk * 16, st.uy + first, b4, bar);
+		bulk_g2s(buf + C * 4, st.ox + first, b4, bar);
+		bulk_g2s(buf + C * 8, st.oy + first, b4, bar);
+		bulk_g2s(buf + C * 12, st.ux + first, b4, bar);
+		bulk_g2s(buf + C * 16, st.uy + first, b4, bar);
 		if(st.id)
-			bulk_g2s(buf + kChunk * 20, st.id + first, b4, bar);
+			bulk_g2s(buf + C * 20, st.id + first, b4, bar);
 	}
 
+	// L2 prefetch of the particles [first, first + cnt) of the tile.
+	static __device__ __forceinline__ void stage_prefetch(const PushArgs &a, int s, int64_t first,
+			int cnt)
+	{
+		const StoreMix &st = a.mix[s];
+		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
+		bulk_prefetch_l2(st.cell + first, b4);
+		bulk_prefetch_l2(st.ox + first, b4);
+		bulk_prefetch_l2(st.oy + first, b4);
+		bulk_prefetch_l2(st.ux + first, b4);
+		bulk_prefetch_l2(st.uy + first, b4);
+		if(st.id)
+			bulk_prefetch_l2(st.id + first, b4);
+	}
+
+	template <int C>
 	static __device__ __forceinline__ Rec from_stage(const unsigned char *buf, int j, bool ids)
 	{
 		const float *f = reinterpret_cast<const float *>(buf);
 		Rec r;
 		r.cell = reinterpret_cast<const int32_t *>(buf)[j];
-		r.ox = f[kChunk + j]; r.oy = f[2 * kChunk + j];
-		r.ux = f[3 * kChunk + j]; r.uy = f[4 * kChunk + j];
-		r.id = ids ? reinterpret_cast<const int32_t *>(buf)[5 * kChunk + j] : 0;
+		r.ox = f[C + j]; r.oy = f[2 * C + j];
+		r.ux = f[3 * C + j]; r.uy = f[4 * C + j];
+		r.id = ids ? reinterpret_cast<const int32_t *>(buf)[5 * C + j] : 0;
 		return r;
 	}
 
@@ -689,10 +723,13 @@ struct Mix {
 // ============================================================== kernels
 
 // Ids: whether the species' store keeps particle ids (always for F64).
-template <class F, int MinBlocks = F::kMinBlocks, bool Ids = true>
+// P: particles per thread per chunk (a chunk is kPushThreads * P particles).
+template <class F, int MinBlocks = F::kMinBlocks, bool Ids = true, int P = kPPT>
 __global__ void __launch_bounds__(kPushThreads, MinBlocks)
 k_push(const PushArgs a)
 {
+	constexpr int kChunk = chunk_of(P);
+	constexpr int kCheckChunks = check_chunks(P);
 	// dynamic shared memory: two staged chunks, then the form's area
 	extern __shared__ __align__(128) unsigned char smem[];
 	__shared__ __align__(8) uint64_t bars[2];
@@ -721,7 +758,7 @@ k_push(const PushArgs a)
 	const int tx0 = (t & (g.ntx - 1)) << g.ltx;
 	const int ty0 = (t >> (g.lnx - g.ltx)) << g.lty;
 	const bool ids = Ids;
-	const size_t sb = F::stage_bytes(ids);
+	const size_t sb = F::stage_bytes(ids, kChunk);
 	// bulk-copy destinations need 16-byte alignment; the host adds 128
 	// bytes of slack for this round-up.  An offset from smem (not a pointer
 	// rebuilt from an integer) keeps every derived pointer in the shared
@@ -758,7 +795,11 @@ k_push(const PushArgs a)
 	}
 	__syncthreads();
 	if(threadIdx.x == 0 && nchunks > 0)
-		F::stage_issue(a, s, base, min(kChunk, n), stage0, &bars[0]);
+	{
+		F::template stage_issue<kChunk>(a, s, base, min(kChunk, n), stage0, &bars[0]);
+		for(int c = 1; c <= kPrefetchChunks && c < nchunks; c++)
+			F::stage_prefetch(a, s, base + c * kChunk, min(kChunk, n - c * kChunk));
+	}
 	const int lane = threadIdx.x & 31;
 
 	for(int ci = 0; ci < nchunks; ci++)
@@ -784,8 +825,12 @@ k_push(const PushArgs a)
 			if(ci >= 1 && !mbar_wait_bounded(&ebars[b], ((ci - 1) >> 1) & 1, a.status))
 				s_timeout = 1;
 			fence_proxy_async_smem();
-			F::stage_issue(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
+			F::template stage_issue<kChunk>(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
 					stage0 + b * sb, &bars[b]);
+			// keep kPrefetchChunks more chunks on their way into L2
+			const int cp = ci + 1 + kPrefetchChunks;
+			if(kPrefetchChunks > 0 && cp < nchunks)
+				F::stage_prefetch(a, s, base + cp * kChunk, min(kChunk, n - cp * kChunk));
 		}
 		// this chunk has landed: every global read of slots below
 		// c0 + kChunk is complete, so the in-place writes below are safe
@@ -793,20 +838,20 @@ k_push(const PushArgs a)
 		if(!mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status))
 			s_timeout = 1;
 		const unsigned char *buf = stage0 + (ci & 1) * sb;
-		typename F::Rec rec[kPPT];
-		int dest[kPPT];
-		unsigned bs[kPPT];
-		Resv rv[kPPT];
+		typename F::Rec rec[P];
+		int dest[P];
+		unsigned bs[P];
+		Resv rv[P];
 		uint32_t err = 0;
 		#pragma unroll
-		for(int k = 0; k < kPPT; k++)
+		for(int k = 0; k < P; k++)
 		{
 			const int j = k * kPushThreads + threadIdx.x;
 			const bool valid = c0 + j < n;
 			dest[k] = -1;
 			if(valid)
 			{
-				rec[k] = F::from_stage(buf, j, ids);
+				rec[k] = F::template from_stage<kChunk>(buf, j, ids);
 				typename F::Out o = F::push(a, s, rec[k], tx0, ty0, Etile);
 				err |= o.err;
 				F::deposit(a, s, fsm, W, H, tx0, ty0, o);
@@ -825,7 +870,7 @@ k_push(const PushArgs a)
 		// one shared-cursor reservation per warp for all its stayers
 		int nst = 0;
 		#pragma unroll
-		for(int k = 0; k < kPPT; k++) nst += __popc(bs[k]);
+		for(int k = 0; k < P; k++) nst += __popc(bs[k]);
 		int wb = 0;
 		if(lane == 0 && nst)
 			wb = atomicAdd(&s_cursor, nst);
@@ -833,7 +878,7 @@ k_push(const PushArgs a)
 		// one store per particle: its own tile's compacted prefix, or its
 		// slot in the destination tile, or the spill list
 		#pragma unroll
-		for(int k = 0; k < kPPT; k++)
+		for(int k = 0; k < P; k++)
 		{
 			const bool stay = (bs[k] >> lane) & 1u;
 			const bool move = dest[k] >= 0 && dest[k] != t;

@@ -51,7 +51,8 @@ enum cpic_status {
 
 /* Simulation parameters; the .conf key each field comes from is named.
  * Defaults for zero fields: plasma_chunks 1, tile and halo chosen by the
- * autotuner. */
+ * library, 2 particles per thread.  No reference counterpart for the last
+ * four (the reference's blocks are MPI ranks and plasma chunks). */
 typedef struct cpic_params {
 	int64_t nx, ny;          /* grid.points */
 	double Lx, Ly;           /* simulation.space_length */
@@ -64,7 +65,8 @@ typedef struct cpic_params {
 	int32_t tile_x, tile_y;  /* cells per tile, powers of two; 0 = auto */
 	int32_t halo;            /* deposit halo in cells; 0 = auto */
 	int32_t track_ids;       /* keep a particle id per particle (MIXED) */
-	int32_t reserved[7];
+	int32_t particles_per_thread; /* fused kernel instance: 1, 2 or 4; 0 = 2 */
+	int32_t reserved[6];
 } cpic_params_t;
 
 typedef struct cpic_ctx cpic_ctx_t;
@@ -189,6 +191,14 @@ CPIC_API int cpic_time_steps(cpic_ctx_t *ctx, int64_t nsteps, double *ms_total,
  * Changes no device setting. */
 CPIC_API int cpic_fp64_peak(int64_t iters, double *gflops, double *ms);
 
+/* No counterpart in the reference (its particle blocks grow and shrink by
+ * list).  Re-lays the particle store out with `slack_pct` percent of spare
+ * capacity per tile (a counting-sort rebuild from the current state; the
+ * particles and their order within a tile are kept).  Tile overflows double
+ * the slack up to 200 %; a run whose particles have spread out again can
+ * compact its store back.  Synchronous. */
+CPIC_API int cpic_compact(cpic_ctx_t *ctx, int32_t slack_pct);
+
 /* Tile geometry chosen for this context: out[4] = {tile_x, tile_y, halo,
  * capacity slack in percent}. */
 CPIC_API int cpic_tile_info(const cpic_ctx_t *ctx, int32_t *out);
@@ -247,6 +257,13 @@ CPIC_API int cpic_ensemble_run(cpic_ensemble_t *e, int64_t nsteps, double *ms_gr
  * per cell, precision) for the process. */
 CPIC_API int cpic_autotune_tile(const cpic_params_t *p, int64_t n, double v0, double vth,
 		int32_t *tile, double *ms_per_step);
+
+/* Autotuner over the whole layout: the tile size and the fused kernel's
+ * particles per thread (its compiled instances: 1, 2 or 4 particles per
+ * thread and chunk, i.e. chunks of 256, 512 or 1024 particles staged per
+ * block), timed together as cpic_autotune_tile does; same cache rule. */
+CPIC_API int cpic_autotune_layout(const cpic_params_t *p, int64_t n, double v0, double vth,
+		int32_t *tile, int32_t *particles_per_thread, double *ms_per_step);
 
 /* --- adjoint: gradient of the final field energy ---------------------- */
 
