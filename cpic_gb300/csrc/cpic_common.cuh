@@ -33,14 +33,7 @@ constexpr int kMaxSpecies = 8;
 #ifndef CPIC_PPT
 #define CPIC_PPT 2
 #endif
-// Chunks of a tile requested into L2 ahead of the one being staged into
-// shared memory (0: none), so that more of the tile is in flight than the
-// two shared-memory buffers hold.
-#ifndef CPIC_PREFETCH_CHUNKS
-#define CPIC_PREFETCH_CHUNKS 2
-#endif
 constexpr int kPushThreads = CPIC_PUSH_THREADS;
-constexpr int kPrefetchChunks = CPIC_PREFETCH_CHUNKS;
 // Particles per thread per chunk: the default, and the compiled instances of
 // the fused kernel a context may choose from (the autotuner times them).
 constexpr int kPPT = CPIC_PPT;
@@ -325,14 +318,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 {
 	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
 			:: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
-}
-
-// Hint to bring [src, src + bytes) of global memory into L2 (src 16-byte
-// aligned, bytes a multiple of 16).  Nothing waits for it; a later bulk copy
-// of the same bytes then reads from L2.
-__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes)
-{
-	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)

@@ -96,20 +96,6 @@ struct F64 {
 		bulk_g2s(buf + C * 32, st.id + first, b4, bar);
 	}
 
-	// L2 prefetch of the particles [first, first + cnt) of the tile.
-	static __device__ __forceinline__ void stage_prefetch(const PushArgs &a, int s, int64_t first,
-			int cnt)
-	{
-		const StoreF64 &st = a.f64[s];
-		uint32_t b8 = (uint32_t) ((cnt * 8 + 15) & ~15);
-		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
-		bulk_prefetch_l2(st.x + first, b8);
-		bulk_prefetch_l2(st.y + first, b8);
-		bulk_prefetch_l2(st.ux + first, b8);
-		bulk_prefetch_l2(st.uy + first, b8);
-		bulk_prefetch_l2(st.id + first, b4);
-	}
-
 	template <int C>
 	static __device__ __forceinline__ Rec from_stage(const unsigned char *buf, int j, bool)
 	{
@@ -449,21 +435,6 @@ struct Mix {
 			bulk_g2s(buf + C * 20, st.id + first, b4, bar);
 	}
 
-	// L2 prefetch of the particles [first, first + cnt) of the tile.
-	static __device__ __forceinline__ void stage_prefetch(const PushArgs &a, int s, int64_t first,
-			int cnt)
-	{
-		const StoreMix &st = a.mix[s];
-		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
-		bulk_prefetch_l2(st.cell + first, b4);
-		bulk_prefetch_l2(st.ox + first, b4);
-		bulk_prefetch_l2(st.oy + first, b4);
-		bulk_prefetch_l2(st.ux + first, b4);
-		bulk_prefetch_l2(st.uy + first, b4);
-		if(st.id)
-			bulk_prefetch_l2(st.id + first, b4);
-	}
-
 	template <int C>
 	static __device__ __forceinline__ Rec from_stage(const unsigned char *buf, int j, bool ids)
 	{
@@ -795,11 +766,7 @@ k_push(const PushArgs a)
 	}
 	__syncthreads();
 	if(threadIdx.x == 0 && nchunks > 0)
-	{
 		F::template stage_issue<kChunk>(a, s, base, min(kChunk, n), stage0, &bars[0]);
-		for(int c = 1; c <= kPrefetchChunks && c < nchunks; c++)
-			F::stage_prefetch(a, s, base + c * kChunk, min(kChunk, n - c * kChunk));
-	}
 	const int lane = threadIdx.x & 31;
 
 	for(int ci = 0; ci < nchunks; ci++)
@@ -827,10 +794,6 @@ k_push(const PushArgs a)
 			fence_proxy_async_smem();
 			F::template stage_issue<kChunk>(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
 					stage0 + b * sb, &bars[b]);
-			// keep kPrefetchChunks more chunks on their way into L2
-			const int cp = ci + 1 + kPrefetchChunks;
-			if(kPrefetchChunks > 0 && cp < nchunks)
-				F::stage_prefetch(a, s, base + cp * kChunk, min(kChunk, n - cp * kChunk));
 		}
 		// this chunk has landed: every global read of slots below
 		// c0 + kChunk is complete, so the in-place writes below are safe

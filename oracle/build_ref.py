@@ -26,15 +26,17 @@ variant (shipped_portable) that a CPU test checks bit for bit against the
 native one.
 
 Where the tree comes from (ref_root): the directory named by CPIC_REFERENCE
-(default /root/reference) when it exists; there stage() also lays out
-oracle/_ref/tree/ (git-ignored, never committed), the view of the tree's
-src/, include/, test/ and conf/ that the builds on the GPU host use, where
-the reference tree itself is absent.  The reference tree is read, never
-written.
+(default /root/reference) when it exists; there stage() also copies the
+tree's src/, include/, test/ and conf/ into oracle/_ref/tree/, the build
+input of the same builds on the GPU host, where the reference tree itself
+is absent.  oracle/_ref/ is git-ignored: the copy is never committed, and it
+is refreshed from the tree at every build here.  The reference tree is read,
+never written.
 """
 import concurrent.futures as cf
 import os
 import platform
+import shutil
 import subprocess
 import sys
 
@@ -62,9 +64,9 @@ def cflags(portable):
 
 
 def stage():
-    """Lays out oracle/_ref/tree/ from the reference tree: one symlink per
-    file of its src/, include/, test/ and conf/ (data files included).
-    Returns the staged root, or None when the reference tree is absent."""
+    """Copies the reference tree's src/, include/, test/ and conf/ (data
+    files included) into oracle/_ref/tree/.  Returns the staged root, or
+    None when the reference tree is absent."""
     if not os.path.isdir(os.path.join(REF, "src")):
         return None
     for d in STAGED_DIRS:
@@ -79,7 +81,7 @@ def stage():
                 dst = os.path.join(dst_d, f)
                 if os.path.lexists(dst):
                     os.remove(dst)
-                os.symlink(os.path.join(dirpath, f), dst)
+                shutil.copy2(os.path.join(dirpath, f), dst)
     return TREE
 
 
@@ -130,7 +132,9 @@ def build(force=False):
     if ref is None:
         return None
     os.makedirs(OUT, exist_ok=True)
-    stamp = os.path.join(OUT, "built.txt")
+    # one stamp per host architecture: the copy of this directory on the GPU
+    # host carries the stamp of this one but none of its binaries
+    stamp = os.path.join(OUT, "built_%s.txt" % platform.machine())
     if os.path.exists(stamp) and not force:
         return OUT
     inc = ["-I", os.path.join(HERE, "shims"), "-I", os.path.join(ROOT, "include"),

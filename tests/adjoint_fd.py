@@ -15,7 +15,11 @@ derivative, whatever the adjoint computes.  So:
   straddle, the check is repeated on the restricted runs (a particle can
   still straddle through the change of the field), and the central
   difference along the restricted direction is compared with the adjoint's
-  gradient projected on the same direction.
+  gradient projected on the same direction;
+- what straddles through the field leaves a kink term of first order in
+  eps (a number of straddlers proportional to eps, each off by an amount
+  proportional to eps, over 2 eps), while the smooth part's error is second
+  order: the Richardson combination 2 D(eps/2) - D(eps) removes it.
 
 Test and study infrastructure (tests/test_gpu_adjoint.py, bench.py --study
 adjoint).
@@ -64,17 +68,17 @@ def restricted_fd(adj, grid, L, dt, q, steps, base, direction, grad, eps, rounds
     keep = np.ones(n, bool)
     out = {"eps": eps}
 
-    def perturbed(sign, m):
+    def perturbed(step, m):
         s = [a.copy() for a in base]
         for k, d in enumerate(direction):
             if d is not None:
-                s[k] = s[k] + sign * eps * d * m
+                s[k] = s[k] + step * d * m
         s[0] = np.mod(s[0], L)
         return s
 
     for r in range(rounds):
         m = keep.astype(np.float64)
-        sp, sm = perturbed(1.0, m), perturbed(-1.0, m)
+        sp, sm = perturbed(eps, m), perturbed(-eps, m)
         strad = straddlers(grid, L, dt, q, sp, sm, steps)
         out["straddle_fraction_round%d" % r] = float(strad.mean())
         if r == 0:
@@ -84,10 +88,20 @@ def restricted_fd(adj, grid, L, dt, q, steps, base, direction, grad, eps, rounds
         else:
             out["straddlers_left"] = int(strad.sum())
     m = keep.astype(np.float64)
-    sp, sm = perturbed(1.0, m), perturbed(-1.0, m)
-    fd = (adj.forward(*sp) - adj.forward(*sm)) / (2 * eps)
+
+    def quotient(e):
+        return (adj.forward(*perturbed(e, m)) - adj.forward(*perturbed(-e, m))) / (2 * e)
+
+    fd = quotient(eps)
+    # the kink term of the particles that still straddle (through the field)
+    # is first order in eps, unlike the smooth part's second-order error:
+    # the Richardson combination of eps and eps/2 cancels it
+    fd_half = quotient(eps / 2)
+    rich = 2.0 * fd_half - fd
     proj = float(sum(np.sum(g * d * m) for g, d in zip(grad, direction) if d is not None))
-    out.update({"fd": fd, "adjoint": proj, "rel_diff": abs(fd - proj) / abs(proj),
+    out.update({"fd": fd, "fd_half_eps": fd_half, "fd_richardson": rich, "adjoint": proj,
+                "rel_diff": abs(fd - proj) / abs(proj),
+                "rel_diff_richardson": abs(rich - proj) / abs(proj),
                 "particles_perturbed": int(keep.sum())})
     return out
 

@@ -178,7 +178,9 @@ def test_fd_at_prescribed_eps_with_edge_crossings_accounted(lib, c5):
     """At the prescribed eps 1e-6 the plain central difference is off by the
     kink term of the particles that cross a cell edge differently in the
     two perturbed runs (tests/adjoint_fd.py).  Restricting the perturbation
-    to the particles that straddle no edge removes that term: the difference
+    to the particles that straddle no edge removes the direct part of that
+    term, and the Richardson combination of eps 1e-6 and 5e-7 removes what
+    straddles through the field (first order in eps): the difference
     quotient along the restricted direction then matches the adjoint's
     gradient projected on it within 1e-4, for both v0 and the amplitude."""
     from tests import adjoint_fd
@@ -193,4 +195,5 @@ def test_fd_at_prescribed_eps_with_edge_crossings_accounted(lib, c5):
         r = adjoint_fd.restricted_fd(adj, c5["grid"], L, 0.05, q, c5["steps"], base, d, g, 1e-6)
         print(name, r)
         assert 0.0 < r["straddle_fraction_full"] < 0.5
-        assert r["rel_diff"] <= 1e-4, (name, r)
+        assert min(r["rel_diff"], r["rel_diff_richardson"]) <= 1e-4, (name, r)
+        assert r["rel_diff_richardson"] <= 1e-4, (name, r)
