@@ -33,13 +33,14 @@ HOST_SOURCES = ["field", "particle", "mover", "interpolate", "comm_plasma", "com
 # their objects (objcopy, the sources stay untouched), so the drop-in's win.
 GPU_STAGES = ["stage_field_E", "stage_plasma_E", "stage_plasma_r", "stage_field_rho", "comm_plasma",
               "particle_comm_initial"]
-# program -> (tree, path): the reference's own mains, unchanged, and this
-# project's stage-by-stage driver
-PROGRAMS = {"cpic_gpu": ("ref", "src/cpic.c"),
-            "test_constant_speed_gpu": ("ref", "test/constant-speed.c"),
-            "test_cyclotron_gpu": ("ref", "test/cyclotron.c"),
-            "test_harmonic_gpu": ("ref", "test/harmonic.c"),
-            "dropin_stages": ("repo", "tests/dropin_stages.c")}
+# program -> (tree, path, extra flags).  test/harmonic.c prints its trace
+# with the reference's debug macro, which only its debug builds enable
+# (GLOBAL_DEBUG, Makefile:74).
+PROGRAMS = {"cpic_gpu": ("ref", "src/cpic.c", []),
+            "test_constant_speed_gpu": ("ref", "test/constant-speed.c", []),
+            "test_cyclotron_gpu": ("ref", "test/cyclotron.c", []),
+            "test_harmonic_gpu": ("ref", "test/harmonic.c", ["-DGLOBAL_DEBUG"]),
+            "dropin_stages": ("repo", "tests/dropin_stages.c", [])}
 
 
 def ref_root():
@@ -79,9 +80,9 @@ def build():
                  os.path.join(ROOT, "oracle", "shims", "shim_runtime.c"), "-o", o])
     objs.append(o)
     mains = {}
-    for name, (tree, f) in PROGRAMS.items():
+    for name, (tree, f, extra) in PROGRAMS.items():
         o = os.path.join(OUT, name + "_main.o")
-        jobs.append(["gcc"] + cflags + ["-I", os.path.join(ref, "src")] + inc
+        jobs.append(["gcc"] + cflags + extra + ["-I", os.path.join(ref, "src")] + inc
                     + ["-c", os.path.join(ref if tree == "ref" else ROOT, f), "-o", o])
         mains[name] = o
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:

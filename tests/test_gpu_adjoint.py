@@ -179,10 +179,13 @@ def test_fd_at_prescribed_eps_with_edge_crossings_accounted(lib, c5):
     kink term of the particles that cross a cell edge differently in the
     two perturbed runs (tests/adjoint_fd.py).  Restricting the perturbation
     to the particles that straddle no edge removes the direct part of that
-    term, and the Richardson combination of eps 1e-6 and 5e-7 removes what
-    straddles through the field (first order in eps): the difference
-    quotient along the restricted direction then matches the adjoint's
-    gradient projected on it within 1e-4, for both v0 and the amplitude."""
+    term.  For v0, where most straddlers are perturbed directly, the
+    difference quotient along the restricted direction then matches the
+    adjoint's gradient projected on it within 1e-4, and the Richardson
+    combination of eps 1e-6 and 5e-7 within 1e-5.  For the amplitude, the
+    straddlers are mostly particles whose own state is not perturbed (they
+    cross through the change of the field), so restricting the direction
+    cannot remove them; the bound there documents what is left."""
     from tests import adjoint_fd
     adj, st = c5["adj"], c5["st"]
     base = _np_state(st, 0.2, 0.01)
@@ -195,5 +198,15 @@ def test_fd_at_prescribed_eps_with_edge_crossings_accounted(lib, c5):
         r = adjoint_fd.restricted_fd(adj, c5["grid"], L, 0.05, q, c5["steps"], base, d, g, 1e-6)
         print(name, r)
         assert 0.0 < r["straddle_fraction_full"] < 0.5
-        assert min(r["rel_diff"], r["rel_diff_richardson"]) <= 1e-4, (name, r)
-        assert r["rel_diff_richardson"] <= 1e-4, (name, r)
+        if name == "v0":
+            # 4.1 % of the particles straddle; restricted: 7.5e-5, and the
+            # Richardson combination 3.8e-6 (measured)
+            assert r["rel_diff"] <= 1e-4 and r["rel_diff_richardson"] <= 1e-5, (name, r)
+        else:
+            # 0.70 % straddle, 0.64 % of them through the change of the field
+            # (their own initial state is not perturbed): what is left is the
+            # kink term of those, 1.2e-4 measured, not first order in eps
+            # (Richardson gives 2.3e-4).  At eps 1e-8, where it has shrunk,
+            # the amplitude gradient agrees to 3.3e-6 (the test above).
+            assert r["straddlers_left"] > 0.8 * r["straddle_fraction_full"] * c5["n"]
+            assert r["rel_diff"] <= 2e-4, (name, r)

@@ -5,8 +5,9 @@ reference tree or its staged view).
 
 - test/constant-speed.c: |u - u0| <= 1e-10 over its 50,000 cycles
   (test/constant-speed.c:90-91);
-- test/cyclotron.c: the weak check's absolute radius error below its limit
-  (test/cyclotron.c:170-190, 317-322);
+- test/cyclotron.c as shipped (strict check): the reference's own Boris
+  phase lag fails it; the GPU run reports the error the oracle's trajectory
+  gives under the driver's formula (test/cyclotron.c:80-236, 317-322);
 - test/harmonic.c: the x position of electron 0 it prints every cycle
   against the reference's trace (tests/golden/harmonic.npz, from the
   reference build), to the printed precision;
@@ -18,6 +19,7 @@ reference tree or its staged view).
   files; the written fields match the oracle (1e-12 of the max norm after
   the pre-step, field energy 1e-10 over the run).
 """
+import math
 import os
 import re
 import subprocess
@@ -56,9 +58,40 @@ def test_constant_speed_driver(out):
 
 
 def test_cyclotron_driver(out):
+    """test/cyclotron.c as shipped (WEAK_CHECK 0) measures the distance to
+    the analytic orbit point, and the reference's own algorithm fails it:
+    Boris rotates by 2 atan(w dt / 2) instead of w dt per step, so after 5000
+    steps the phase lag puts the particle 0.52 from that point against a
+    limit of v dt^2 = 0.025.  The GPU run must fail the same way, with the
+    error the oracle's trajectory gives under the driver's own formula
+    (cyclotron.c:80-236): 0.523678 there."""
     r = run(out, "test_cyclotron_gpu")
-    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
-    assert re.search(r"^OK .*Absolute error .* is lower than the limit", r.stdout, re.M)
+    m = re.search(r"^FAIL .*The error ([-+0-9.e]+) exceeds the limit ([-+0-9.e]+)", r.stdout, re.M)
+    assert r.returncode == 1 and m, r.stdout[-2000:] + r.stderr[-2000:]
+    err, limit = float(m.group(1)), float(m.group(2))
+    # the same measure on the oracle's trajectory
+    from oracle.oracle import Oracle
+    dt, steps, v, B = 0.05, 5000, 10.0, (0.0, 0.0, -1.0)
+    o = Oracle(4, 4, 32.0, 32.0, dt, 8.85e-12, B, plasma_chunks=4)
+    o.add_species(-1.0, 1.0, [2.0], [16.0], [0.0], [v])
+    o.pre_step()
+    freq = -1.0                      # |q| B_z / m
+    radius = v / freq
+    uxB = np.cross([0.0, v, 0.0], B)
+    center = np.array([2.0, 16.0]) + (uxB * radius / np.linalg.norm(uxB))[:2]
+    worst = 0.0
+    for k in range(steps):
+        o.step()                     # iter k + 1; the driver uses t = k dt
+        x, y, _, _ = o.particles(0)
+        t = k * dt
+        R = radius * np.array([math.cos(t * freq), math.sin(t * freq)])
+        worst = max(worst, float(np.hypot(*(np.array([x[0], y[0]]) - center - R))))
+    o.close()
+    assert limit == pytest.approx(v * dt * dt, rel=1e-6)
+    # the electron's own field cancels at its position only to the FFT's
+    # rounding, which differs between the GPU solver and the oracle's: the
+    # trajectories agree to 1e-4 after 5000 steps (tests/test_gpu_physics.py)
+    assert abs(err - worst) <= 1e-4, (err, worst)
 
 
 def test_harmonic_driver_trace(out):
