@@ -582,12 +582,12 @@ def study_phases(args):
                      "tile_max_over_mean": float(tc.max() / tc.mean()),
                      "tile_p99_over_mean": float(np.quantile(tc, 0.99) / tc.mean()),
                      "field_energy": ctx.field_energy()})
-    # the same state re-laid out with the initial 25 % slack: whether the
+    # the same state re-laid out with 100 % slack (not 200 %): whether the
     # late steps' cost comes from the store's spread (slack grown to 200 %)
     before = ctx.layout_stats()
-    ctx.compact(25)
+    ctx.compact(100)
     t = ctx.time_steps(blk)
-    rows.append({"step": done + blk, "after_compact_to_25pct": True, "slack_before": before["slack_pct"],
+    rows.append({"step": done + blk, "after_compact_to_100pct": True, "slack_before": before["slack_pct"],
                  "ms_step": t["ms_total"] / blk, "ms_push": t["ms_plasma"] / blk,
                  "ms_field": t["ms_field"] / blk, "stats": ctx.layout_stats()})
     ctx.close()
