@@ -803,6 +803,7 @@ static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
 		st.qfix = vq * c->qscale;
 		st.qlo_mul = c->qlo_mul;
 		st.wq_scale = c->wq_exact ? c->sp[s].wq_mult : st.qfix * ldexp(1.0, -kWeightBits);
+		st.wq_int = c->wq_exact ? (long long) c->sp[s].wq_mult : 0;
 		st.dtqm2_f = (float) st.dtqm2;
 		st.tz_f = (float) st.tz;
 		st.sz_f = (float) st.sz;

@@ -575,6 +575,15 @@ struct Mix {
 		return (m >> 30) != 0;
 	}
 
+	// Fixed-point units of v integer weight units: an integer product when
+	// the species' factor is an exact integer (then (double) v * sc is exact
+	// too, so both give the same value; the integer one keeps the FP64 pipe,
+	// narrow on this GPU, out of the deposit's fallback and flush paths).
+	static __device__ __forceinline__ long long wunits(uint32_t v, const SpeciesStep &sp)
+	{
+		return sp.wq_int ? (long long) v * sp.wq_int : __double2ll_rn((double) v * sp.wq_scale);
+	}
+
 	// Add the 32-bit sums to global rho and restart them from zero
 	// (between barriers).  With the species' fixed-point factor an exact
 	// integer, the partial sums add up to exactly the value one flush of
@@ -583,14 +592,13 @@ struct Mix {
 			int W, int H, int tx0, int ty0)
 	{
 		uint32_t *a32 = sh32(sm, W, a.g.tx);
-		double sc = a.sp[s].wq_scale;
+		const SpeciesStep &sp = a.sp[s];
 		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
 		{
 			uint32_t v = a32[i];
 			if(v != 0)
 			{
-				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)],
-						__double2ll_rn((double) v * sc));
+				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)], wunits(v, sp));
 				a32[i] = 0;
 			}
 		}
@@ -610,10 +618,9 @@ struct Mix {
 		}
 		else
 		{
-			double sc = a.sp[s].wq_scale;
-			dep_global(a.rho, a.g, tx0 + o.rx, ty0 + o.ry,
-					__double2ll_rn((double) o.wq[0] * sc), __double2ll_rn((double) o.wq[1] * sc),
-					__double2ll_rn((double) o.wq[2] * sc), __double2ll_rn((double) o.wq[3] * sc));
+			const SpeciesStep &sp = a.sp[s];
+			dep_global(a.rho, a.g, tx0 + o.rx, ty0 + o.ry, wunits(o.wq[0], sp), wunits(o.wq[1], sp),
+					wunits(o.wq[2], sp), wunits(o.wq[3], sp));
 		}
 	}
 
@@ -621,13 +628,12 @@ struct Mix {
 			int W, int H, int tx0, int ty0)
 	{
 		const uint32_t *a32 = sh32(sm, W, a.g.tx);
-		double sc = a.sp[s].wq_scale;
+		const SpeciesStep &sp = a.sp[s];
 		for(int i = threadIdx.x; i < W * W; i += blockDim.x)
 		{
 			uint32_t v = a32[i];
 			if(v != 0)
-				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)],
-						__double2ll_rn((double) v * sc));
+				red_global(&a.rho[frame_node(a.g, W, H, tx0, ty0, i)], wunits(v, sp));
 		}
 	}
 
