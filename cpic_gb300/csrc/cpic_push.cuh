@@ -578,7 +578,9 @@ struct Mix {
 	// Fixed-point units of v integer weight units: an integer product when
 	// the species' factor is an exact integer (then (double) v * sc is exact
 	// too, so both give the same value; the integer one keeps the FP64 pipe,
-	// narrow on this GPU, out of the deposit's fallback and flush paths).
+	// narrow on this GPU, out of the fold and flush; the per-particle global
+	// fallback keeps the FP64 form, which needs fewer registers inside the
+	// particle loop).
 	static __device__ __forceinline__ long long wunits(uint32_t v, const SpeciesStep &sp)
 	{
 		return sp.wq_int ? (long long) v * sp.wq_int : __double2ll_rn((double) v * sp.wq_scale);
@@ -618,9 +620,10 @@ struct Mix {
 		}
 		else
 		{
-			const SpeciesStep &sp = a.sp[s];
-			dep_global(a.rho, a.g, tx0 + o.rx, ty0 + o.ry, wunits(o.wq[0], sp), wunits(o.wq[1], sp),
-					wunits(o.wq[2], sp), wunits(o.wq[3], sp));
+			double sc = a.sp[s].wq_scale;
+			dep_global(a.rho, a.g, tx0 + o.rx, ty0 + o.ry,
+					__double2ll_rn((double) o.wq[0] * sc), __double2ll_rn((double) o.wq[1] * sc),
+					__double2ll_rn((double) o.wq[2] * sc), __double2ll_rn((double) o.wq[3] * sc));
 		}
 	}
 
