@@ -490,52 +490,63 @@ def cpu_baseline(grid, ppc, v0, vth, amp, dt, n_full):
 
 
 def run_reference(args):
-    """The reference's algorithm on the host cores: one oracle process per
-    core, each on the full grid with 1/cores of the workload's particles (so
-    that together they step the workload's particle count), W warm-up steps,
-    then K steps timed together (a barrier starts them).  value = particles
-    stepped by all processes x K / wall time of that window.  Loads no
-    product library and uses no GPU."""
+    """The reference on the host cores, on the workload: one process per core,
+    each on the full grid with 1/cores of the workload's particles (so that
+    together they step the workload's particle count), W warm-up steps, then
+    K steps timed together (a barrier starts them).  value = particles
+    stepped by all processes x K / wall time of that window.  The processes
+    run the reference's own code, built from its sources (oracle/build_ref.py,
+    with the portable intrinsics on the Arm host) when it is built here,
+    else its C restatement, the oracle.  Loads no product library and uses no
+    GPU."""
     ws, rank = dist()
     if rank != 0:
         return None
     grid, ppc, v0, vth, amp, desc = WORKLOADS[args.workload]
-    from oracle import oracle
-    oracle.build()
-    import multiprocessing as mp
+    from oracle import ref_run
     cores = os.cpu_count() or 1
     n_full = grid * grid * ppc
     n = max(1024, n_full // cores)
-    ctx = mp.get_context("spawn")
-    barrier, q = ctx.Barrier(cores), ctx.Queue()
-    procs = [ctx.Process(target=_oracle_replica,
-                         args=(grid, n, v0, vth, amp, 0.05, 99 + i, args.warmup, args.steps, barrier, q))
-             for i in range(cores)]
-    for p in procs:
-        p.start()
-    res = [q.get() for _ in procs]
-    for p in procs:
-        p.join()
-        if p.exitcode != 0:
-            raise RuntimeError("oracle replica failed (exit code %s)" % p.exitcode)
+    L = 2 * math.pi
+    if ref_run.harness() is not None:
+        res = ref_run.time_two_stream(cores, grid, n, v0, vth, amp, 0.05, L, args.warmup, args.steps)
+        res = [(r[0], r[1], r[2], list(r[3]), None) for r in res]
+        kind = "reference"
+        what = ("the reference's own step (src/*.c as shipped, built from its sources against "
+                "single-rank MPI/FFTW/libconfig stand-ins, serial), driven by oracle/ref_harness.c")
+    else:
+        from oracle import oracle
+        oracle.build()
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        barrier, q = ctx.Barrier(cores), ctx.Queue()
+        procs = [ctx.Process(target=_oracle_replica,
+                             args=(grid, n, v0, vth, amp, 0.05, 99 + i, args.warmup, args.steps, barrier, q))
+                 for i in range(cores)]
+        for p in procs:
+            p.start()
+        res = [q.get() for _ in procs]
+        for p in procs:
+            p.join()
+            if p.exitcode != 0:
+                raise RuntimeError("oracle replica failed (exit code %s)" % p.exitcode)
+        kind = "port"
+        what = ("the oracle (FP64 C restatement of the reference step, single threaded; the "
+                "reference itself is not built on this host)")
     window = max(r[2] for r in res) - min(r[1] for r in res)
     total = sum(r[0] for r in res)
     v = total * args.steps / window
     ms_step = window / args.steps * 1e3
     mean_step = statistics.mean(statistics.mean(r[3]) for r in res)
-    sample = ("%d concurrent oracle processes (FP64 C restatement of the reference step, single "
-              "threaded), one per host core, each the full %dx%d grid with %d of the workload's "
-              "particles (%d in all), %d warm-up + %d timed steps; mean step %.3f s per process, "
-              "of which %.3f s field solve" % (cores, grid, grid, n, total, args.warmup, args.steps,
-                                                mean_step, statistics.mean(r[4] for r in res)))
+    sample = ("%d concurrent processes of %s, one per host core, each the full %dx%d grid with "
+              "%d of the workload's particles (%d in all), %d warm-up + %d timed steps; mean step "
+              "%.3f s per process" % (cores, what, grid, grid, n, total, args.warmup, args.steps,
+                                      mean_step))
     return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": DATA, "config": bench_config(grid, ppc, desc),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample + "; the reference's own sources build only on x86-64 "
-                             "(AVX2 intrinsics) against MPI/FFTW/libconfig stand-ins, so its C "
-                             "restatement (pinned bit-exact to that build where it exists) runs"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -646,42 +646,11 @@ orc_poisson(int64_t nx, int64_t ny, const double *rho, double *phi)
  *
  * The seeded two-stream and Maxwellian states of the benchmark workloads,
  * restated here so that the CPU legs of the benchmark build their inputs
- * without the product library.  Same generator as the product's init
- * methods (cpic_gb300/csrc/cpic_init.c): every draw is the SplitMix64
- * finaliser of (stream base + (i + 1) * golden ratio), the top 53 bits
- * scaled to [0, 1); normals by Box-Muller from draws 2i and 2i+1 of a
- * stream; streams 16 * species + {0, 1, 2, 3} are x, y, ux, uy.  A CPU test
- * checks the two bit for bit. */
+ * without the product library.  The generator (seed_init.h) is the product's
+ * init methods' (cpic_gb300/csrc/cpic_init.c); a CPU test checks the two bit
+ * for bit. */
 
-static inline uint64_t
-orc_mix64(uint64_t z)
-{
-	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-	z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-	return z ^ (z >> 31);
-}
-
-#define ORC_GOLDEN 0x9E3779B97F4A7C15ULL
-
-static inline uint64_t
-orc_stream(uint64_t seed, uint64_t stream)
-{
-	return orc_mix64(seed * ORC_GOLDEN + orc_mix64(stream + 0x632BE59BD9B4E019ULL));
-}
-
-static inline double
-orc_unif(uint64_t base, uint64_t i)
-{
-	return (double) (orc_mix64(base + (i + 1) * ORC_GOLDEN) >> 11) * 0x1.0p-53;
-}
-
-static inline double
-orc_gauss(uint64_t base, uint64_t i)
-{
-	double u1 = 1.0 - orc_unif(base, 2 * i);
-	double u2 = orc_unif(base, 2 * i + 1);
-	return sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2);
-}
+#include "seed_init.h"
 
 /* Beams +v0 (first n/2) and -v0 with spread vth; x += amp sin(2 pi x / Lx),
  * wrapped into [0, Lx). */
@@ -689,25 +658,7 @@ void
 orc_init_two_stream(uint64_t seed, int species, int64_t n, double Lx, double Ly,
 		double v0, double vth, double amp, double *x, double *y, double *ux, double *uy)
 {
-	uint64_t s = 16u * (uint64_t) species;
-	uint64_t bx = orc_stream(seed, s + 0), by = orc_stream(seed, s + 1);
-	uint64_t bu = orc_stream(seed, s + 2), bv = orc_stream(seed, s + 3);
-	int64_t i, half = n / 2;
-	for(i = 0; i < n; i++)
-	{
-		double px = orc_unif(bx, (uint64_t) i) * Lx;
-		double py = orc_unif(by, (uint64_t) i) * Ly;
-		if(amp != 0.0)
-		{
-			px = fmod(px + amp * sin(2.0 * M_PI * px / Lx), Lx);
-			if(px < 0.0) px += Lx;
-			if(px >= Lx) px -= Lx;
-		}
-		x[i] = px;
-		y[i] = py;
-		ux[i] = (i < half ? v0 : -v0) + (vth != 0.0 ? vth * orc_gauss(bu, (uint64_t) i) : 0.0);
-		uy[i] = vth != 0.0 ? vth * orc_gauss(bv, (uint64_t) i) : 0.0;
-	}
+	seed_two_stream(seed, species, n, Lx, Ly, v0, vth, amp, x, y, ux, uy);
 }
 
 /* Uniform positions, drifting 2D Maxwellian velocities. */
@@ -716,14 +667,14 @@ orc_init_maxwellian(uint64_t seed, int species, int64_t n, double Lx, double Ly,
 		double vth, double driftx, double drifty, double *x, double *y, double *ux, double *uy)
 {
 	uint64_t s = 16u * (uint64_t) species;
-	uint64_t bx = orc_stream(seed, s + 0), by = orc_stream(seed, s + 1);
-	uint64_t bu = orc_stream(seed, s + 2), bv = orc_stream(seed, s + 3);
+	uint64_t bx = seed_stream(seed, s + 0), by = seed_stream(seed, s + 1);
+	uint64_t bu = seed_stream(seed, s + 2), bv = seed_stream(seed, s + 3);
 	int64_t i;
 	for(i = 0; i < n; i++)
 	{
-		x[i] = orc_unif(bx, (uint64_t) i) * Lx;
-		y[i] = orc_unif(by, (uint64_t) i) * Ly;
-		ux[i] = driftx + vth * orc_gauss(bu, (uint64_t) i);
-		uy[i] = drifty + vth * orc_gauss(bv, (uint64_t) i);
+		x[i] = seed_unif(bx, (uint64_t) i) * Lx;
+		y[i] = seed_unif(by, (uint64_t) i) * Ly;
+		ux[i] = driftx + vth * seed_gauss(bu, (uint64_t) i);
+		uy[i] = drifty + vth * seed_gauss(bv, (uint64_t) i);
 	}
 }

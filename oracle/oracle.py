@@ -22,7 +22,7 @@ _LIB = None
 
 def build(force=False):
     """Compile the oracle with the reference's FP semantics (no contraction)."""
-    deps = [SRC, os.path.join(HERE, "orc_fft.h")]
+    deps = [SRC, os.path.join(HERE, "orc_fft.h"), os.path.join(HERE, "seed_init.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)

@@ -18,11 +18,25 @@
  * A dump: int64 nx, ny, nspecies; rho (ny x nx), phi (ny x nx), Ex, Ey
  * ((ny+1) x nx); per species: int64 n, then for every particle in the
  * plist order: int64 id, x, y, ux, uy, Ex, Ey.
+ *
+ * Timing mode (the CPU arm of the benchmark): STATE_IN of the form
+ * "two_stream:SEED:V0:VTH:AMP" generates every species' state with the
+ * seeded two-stream generator (seed_init.h, the product's init method)
+ * instead of reading a file; NSTEPS is "WARMUP+STEPS".  After the pre-step
+ * and WARMUP untimed steps the harness creates OUT_DIR/ready.<pid> and waits
+ * for OUT_DIR/go (so that concurrent harnesses time the same window), then
+ * times STEPS calls of sim_step and writes OUT_DIR/times.<pid>: int64
+ * particles, then CLOCK_MONOTONIC seconds (double) before the first and
+ * after every timed step.  No dumps in this mode.
  */
 #define _GNU_SOURCE
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
+#include <unistd.h>
+
+#include "seed_init.h"
 
 #include "def.h"
 #include "sim.h"
@@ -108,6 +122,54 @@ field_energy(sim_t *sim)
 	return 0.5 * sim->e0 * we * sim->dx[X] * sim->dx[Y];
 }
 
+static double
+now(void)
+{
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return (double) ts.tv_sec + 1e-9 * (double) ts.tv_nsec;
+}
+
+/* Timing mode: WARMUP untimed steps, the barrier through OUT_DIR, STEPS
+ * timed steps. */
+static int
+time_steps(sim_t *sim, const char *dir, const char *spec)
+{
+	long long warm = 0, steps = 0, k, n = 0;
+	char path[4096];
+	FILE *f;
+	int is;
+	if(sscanf(spec, "%lld+%lld", &warm, &steps) != 2 || steps <= 0) die_msg("NSTEPS: WARMUP+STEPS");
+	for(k = 0; k < warm; k++)
+		if(sim_step(sim)) die_msg("sim_step failed");
+	for(is = 0; is < (int) sim->nspecies; is++) n += sim->species[is].nparticles;
+	snprintf(path, sizeof(path), "%s/ready.%d", dir, (int) getpid());
+	if(!(f = fopen(path, "w"))) die_msg("cannot write ready file");
+	fclose(f);
+	snprintf(path, sizeof(path), "%s/go", dir);
+	for(k = 0; access(path, F_OK) != 0; k++)
+	{
+		if(k > 6000000) die_msg("no go signal");   /* 10 min of 100 us naps */
+		usleep(100);
+	}
+	double *t = malloc(sizeof(double) * (size_t) (steps + 1));
+	if(!t) die_msg("out of memory");
+	t[0] = now();
+	for(k = 0; k < steps; k++)
+	{
+		if(sim_step(sim)) die_msg("sim_step failed");
+		t[k + 1] = now();
+	}
+	snprintf(path, sizeof(path), "%s/times.%d", dir, (int) getpid());
+	if(!(f = fopen(path, "wb"))) die_msg("cannot write times");
+	int64_t n64 = n;
+	wr(f, &n64, 8);
+	wr(f, t, sizeof(double) * (size_t) (steps + 1));
+	fclose(f);
+	free(t);
+	return 0;
+}
+
 int
 main(int argc, char *argv[])
 {
@@ -124,17 +186,26 @@ main(int argc, char *argv[])
 	sim = sim_init(&conf, 1);
 	if(!sim) die_msg("sim_init failed");
 
-	f = fopen(argv[2], "rb");
-	if(!f) die_msg("cannot open state");
+	unsigned long long gseed = 0;
+	double gv0 = 0.0, gvth = 0.0, gamp = 0.0;
+	int timing = sscanf(argv[2], "two_stream:%llu:%lf:%lf:%lf", &gseed, &gv0, &gvth, &gamp) == 4;
+	f = timing ? NULL : fopen(argv[2], "rb");
+	if(!timing && !f) die_msg("cannot open state");
 	for(is = 0; is < sim->nspecies; is++)
 	{
 		int64_t n, ic;
 		double *x, *y, *ux, *uy;
-		if(fread(&n, 8, 1, f) != 1) die_msg("short state");
+		if(timing)
+			n = sim->species[is].nparticles;
+		else if(fread(&n, 8, 1, f) != 1)
+			die_msg("short state");
 		if(n != sim->species[is].nparticles) die_msg("particle count differs from conf");
 		x = malloc(8 * (size_t) n); y = malloc(8 * (size_t) n);
 		ux = malloc(8 * (size_t) n); uy = malloc(8 * (size_t) n);
-		if(fread(x, 8, (size_t) n, f) != (size_t) n || fread(y, 8, (size_t) n, f) != (size_t) n
+		if(!x || !y || !ux || !uy) die_msg("out of memory");
+		if(timing)
+			seed_two_stream(gseed, (int) is, n, sim->L[X], sim->L[Y], gv0, gvth, gamp, x, y, ux, uy);
+		else if(fread(x, 8, (size_t) n, f) != (size_t) n || fread(y, 8, (size_t) n, f) != (size_t) n
 				|| fread(ux, 8, (size_t) n, f) != (size_t) n
 				|| fread(uy, 8, (size_t) n, f) != (size_t) n)
 			die_msg("short state");
@@ -158,13 +229,15 @@ main(int argc, char *argv[])
 		}
 		free(x); free(y); free(ux); free(uy);
 	}
-	fclose(f);
+	if(f) fclose(f);
 
 	/* the pre-step on the injected state, sim.c:208-236 (iter is 0 here;
 	 * the exchange tags only need to be consistent) */
 	particle_comm_initial(sim);
 	stage_field_rho(sim);
 	stage_field_E(sim);
+	if(timing)
+		return time_steps(sim, argv[3], argv[4]);
 	snprintf(path, sizeof(path), "%s/pre.bin", argv[3]);
 	dump(sim, path);
 

@@ -8,6 +8,8 @@ import tempfile
 
 import numpy as np
 
+from oracle.ref_run import write_conf  # noqa: F401  (the .conf of a case)
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF_OUT = os.path.join(ROOT, "oracle", "_ref")
 
@@ -18,49 +20,6 @@ def available():
     except ImportError:
         return False
     return build_ref.build() is not None
-
-
-def write_conf(path, case, cycles):
-    """A .conf with the keys sim_read_config requires (src/sim.c:51-84);
-    particles are placed by the harness, so the init method is a
-    placeholder."""
-    sp = []
-    for s in case["species"]:
-        sp.append("""	{
-		name = "s"
-		particles = %d
-		charge = %r
-		mass = %r
-		drift_velocity = [0.0, 0.0]
-		init_method = "position delta"
-		position_delta = [0.0, 0.0]
-		position_init = [0.0, 0.0]
-	}""" % (len(s["x"]), float(s["q"]), float(s["m"])))
-    L = float(case["L"])
-    txt = """species = (
-%s
-)
-field = { magnetic = [%r, %r, %r] }
-grid = { points = [%d, %d] }
-simulation = {
-	dimensions = 2
-	solver = "MFT"
-	enable_fftw_threads = 0
-	plasma_chunks = 1
-	random_seed = 1
-	cycles = %d
-	time_step = %r
-	space_length = [%r, %r]
-	sampling_period = { energy = 0; field = 0; particle = 0 }
-	stop_SEM = 0.0
-	realtime_plot = 0
-	pblock_nmax = 1024
-}
-constants = { light_speed = 1.0; vacuum_permittivity = 1.0 }
-""" % (",\n".join(sp), float(case["B"][0]), float(case["B"][1]), float(case["B"][2]), case["nx"],
-       case["ny"], cycles, float(case["dt"]), L, L)
-    with open(path, "w") as f:
-        f.write(txt)
 
 
 def write_state(path, case):
