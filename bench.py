@@ -601,6 +601,25 @@ def study_phases(args):
     rows.append({"step": done + blk, "after_compact_to_100pct": True, "slack_before": before["slack_pct"],
                  "ms_step": t["ms_total"] / blk, "ms_push": t["ms_plasma"] / blk,
                  "ms_field": t["ms_field"] / blk, "stats": ctx.layout_stats()})
+    # the same particles uploaded again into a fresh context: the upload sort
+    # orders every tile's particles by direction of motion, in place of the
+    # order the in-place re-bin has accumulated (arrival order); the steps
+    # after it show what that order costs (timing only: the new context's
+    # iteration 0 is a half kick)
+    n = ctx.counts[0]
+    L = 2 * math.pi
+    x, y, ux, uy = ctx.particles(0)
+    ctx.close()
+    q = -L * L / n
+    ctx = make_ctx(grid, {"L": L}, _lib.MIXED, 0.05)
+    ctx.add_species(q, -q, x, y, ux, uy)
+    del x, y, ux, uy
+    ctx.pre_step()
+    ctx.run(1)
+    t = ctx.time_steps(blk)
+    rows.append({"step": done + 2 * blk + 1, "after_reupload": True, "ms_step": t["ms_total"] / blk,
+                 "ms_push": t["ms_plasma"] / blk, "ms_field": t["ms_field"] / blk,
+                 "stats": ctx.layout_stats()})
     ctx.close()
     return {"study": "phases", "workload": desc, "tile": T, "rows": rows}
 
