@@ -1077,16 +1077,14 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 		CK(cudaMalloc(&cur, std::max(nrow, 2 * nt) * sizeof(unsigned long long)));
 		CK(cudaMemcpyAsync(cur, rowcur.data(), nrow * sizeof(unsigned long long),
 				cudaMemcpyHostToDevice, st));
-		static bool pattr = false;
-		if(!pattr)
-		{
+		static PerDeviceOnce pass_once;
+		CK(pass_once.run([] {
 			const int mm = (int) rb_smem_bytes<Mix>(), mf = (int) rb_smem_bytes<F64>();
-			cudaFuncSetAttribute(k_rb_pass<Mix, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mm);
-			cudaFuncSetAttribute(k_rb_pass<F64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mf);
-			cudaFuncSetAttribute(k_rb_pass<Mix, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mm);
-			cudaFuncSetAttribute(k_rb_pass<F64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mf);
-			pattr = true;
-		}
+			cudaError_t e = set_max_dyn_smem({(const void *) k_rb_pass<Mix, true>,
+					(const void *) k_rb_pass<Mix, false>}, mm);
+			return e != cudaSuccess ? e : set_max_dyn_smem({(const void *) k_rb_pass<F64, true>,
+					(const void *) k_rb_pass<F64, false>}, mf);
+		}));
 		const int pb = 152 * 2;
 		const size_t smm = rb_smem_bytes<Mix>(), smf = rb_smem_bytes<F64>();
 		if(mix)
