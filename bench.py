@@ -608,13 +608,17 @@ def study_phases(args):
     # iteration 0 is a half kick)
     n = ctx.counts[0]
     L = 2 * math.pi
+    H = ctx.tile_info()["halo"]
     x, y, ux, uy = ctx.particles(0)
     ctx.close()
     q = -L * L / n
-    ctx = make_ctx(grid, {"L": L}, _lib.MIXED, 0.05)
+    # same tile, halo (so the same resident blocks per SM) and slack
+    ctx = _lib.Context(grid, grid, L, L, 0.05, 1.0, (0.0, 0.0, 0.0), precision=_lib.MIXED,
+                       track_ids=False, tile=T, halo=H)
     ctx.add_species(q, -q, x, y, ux, uy)
     del x, y, ux, uy
     ctx.pre_step()
+    ctx.compact(200)
     ctx.run(1)
     t = ctx.time_steps(blk)
     rows.append({"step": done + 2 * blk + 1, "after_reupload": True, "ms_step": t["ms_total"] / blk,

@@ -342,6 +342,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 	return ok != 0;
 }
 
+#ifndef CPIC_WAIT_MODE
+#define CPIC_WAIT_MODE 0
+#endif
+
+__device__ __forceinline__ bool mbar_try_wait_nohint(uint64_t *bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\t"
+			"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+	return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\t"
+			"mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+	return ok != 0;
+}
+
 // Polls of a bounded mbarrier wait before it gives up (about 1.6 s with
 // the suspend hint above).
 constexpr uint32_t kWaitPolls = 1u << 14;
@@ -353,9 +377,24 @@ constexpr uint32_t kWaitPolls = 1u << 14;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *status,
 		uint32_t polls = kWaitPolls)
 {
+#if CPIC_WAIT_MODE == 1
+	for(uint32_t it = 0; it < polls * 64u; it++)
+		if(mbar_try_wait_nohint(bar, parity))
+			return true;
+#elif CPIC_WAIT_MODE == 2
+	uint32_t ns = 32;
+	for(uint32_t it = 0; it < polls * 256u; it++)
+	{
+		if(mbar_test_wait(bar, parity))
+			return true;
+		__nanosleep(ns);
+		if(ns < 512) ns <<= 1;
+	}
+#else
 	for(uint32_t it = 0; it < polls; it++)
 		if(mbar_try_wait(bar, parity))
 			return true;
+#endif
 	set_status(status, ST_TIMEOUT);
 	return false;
 }
