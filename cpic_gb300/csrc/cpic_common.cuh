@@ -109,6 +109,7 @@ struct SpeciesStep {
 	double umax_x, umax_y;
 	double qfix;         // fixed-point units per unit of w: -q/e0 * qscale
 	double qlo_mul;      // FP64 form: 2^m, the scale of the remainder word
+	int qlo_exp;         // m
 	double wq_scale;     // mixed: fixed-point units per integer weight unit
 	long long wq_int;    // the same as an integer when it is one, else 0
 	float dtqm2_f, tz_f, sz_f;

@@ -802,6 +802,7 @@ static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
 		double vq = -q / p.e0;
 		st.qfix = vq * c->qscale;
 		st.qlo_mul = c->qlo_mul;
+		st.qlo_exp = ilogb(c->qlo_mul);
 		st.wq_scale = c->wq_exact ? c->sp[s].wq_mult : st.qfix * ldexp(1.0, -kWeightBits);
 		st.wq_int = c->wq_exact ? (long long) c->sp[s].wq_mult : 0;
 		st.dtqm2_f = (float) st.dtqm2;

@@ -25,6 +25,7 @@
 // the end of chunk k, all of which were read before the barrier.
 #pragma once
 #include "cpic_common.cuh"
+#include "cpic_bits.h"
 
 namespace cpic {
 
@@ -109,12 +110,19 @@ struct F64 {
 	// relative_position_grid, interpolate.c:38-66 (field origin 0 on one
 	// rank).  The cell index is floor() converted to int, as
 	// vf64_to_vi64 does for in-range values (simd_avx2.h:238-248).
+	// The floor and its conversion to int are done on the integer pipe
+	// (cpic_bits.h, exact) for positions in the box, the FP64 instructions
+	// otherwise.
 	static __device__ __forceinline__ double rel_pos(double x, double dx, double idx, int &i0)
 	{
 		double block_delta = x - 0.0;
 		double block_rel = block_delta * idx;
-		double block_start = floor(block_rel);
-		i0 = (int) block_start;
+		double block_start;
+		if(!bits::floor_nonneg(block_rel, block_start, i0))
+		{
+			block_start = floor(block_rel);
+			i0 = (int) block_start;
+		}
 		double grid_delta = block_delta - block_start * dx;
 		return grid_delta * idx;
 	}
@@ -226,9 +234,16 @@ struct F64 {
 		for(int c = 0; c < 4; c++)
 		{
 			double v = w[c] * sp.qfix;
-			long long hi = __double2ll_rn(v);
+			// the split on the integer pipe (cpic_bits.h: exact, the same
+			// values), the FP64 instructions for what it does not take
+			long long hi, lo;
+			if(!bits::split_fixed(v, sp.qlo_exp, hi, lo))
+			{
+				hi = __double2ll_rn(v);
+				lo = __double2ll_rn((v - (double) hi) * sp.qlo_mul);
+			}
 			o.w[c] = hi;
-			o.wl[c] = __double2ll_rn((v - (double) hi) * sp.qlo_mul);
+			o.wl[c] = lo;
 		}
 		if(i0x >= g.nx || i0y >= g.ny || i0x < 0 || i0y < 0)
 		{
