@@ -327,27 +327,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(bar)) : "memory");
 }
 
-// A waiting thread may be suspended up to this long (it wakes as soon as
-// the phase completes): fewer polls, fewer issue slots taken from the
-// warps that have work.  With the iteration limit below, a wait gives up
-// after at most about 1.6 s.
-constexpr uint32_t kWaitHintNs = 100000;
-
+// One probe of the mbarrier phase of the given parity.  The thread may be
+// suspended for a hardware-defined time limit while the phase is pending
+// (it wakes as soon as the phase completes).  Measured on the fused kernel
+// (2048^2, 20 steps, 3 alternating rounds): 3.643 ms per launch, against
+// 3.667 ms with an explicit 100 us suspend-time hint and 3.711 ms with
+// test_wait and an exponential nanosleep backoff.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
-{
-	uint32_t ok;
-	asm volatile("{\n\t.reg .pred p;\n\t"
-			"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-			"selp.u32 %0, 1, 0, p;\n\t}"
-			: "=r"(ok) : "r"(smem_addr(bar)), "r"(parity), "r"(kWaitHintNs) : "memory");
-	return ok != 0;
-}
-
-#ifndef CPIC_WAIT_MODE
-#define CPIC_WAIT_MODE 0
-#endif
-
-__device__ __forceinline__ bool mbar_try_wait_nohint(uint64_t *bar, uint32_t parity)
 {
 	uint32_t ok;
 	asm volatile("{\n\t.reg .pred p;\n\t"
@@ -357,19 +343,10 @@ __device__ __forceinline__ bool mbar_try_wait_nohint(uint64_t *bar, uint32_t par
 	return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity)
-{
-	uint32_t ok;
-	asm volatile("{\n\t.reg .pred p;\n\t"
-			"mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-			"selp.u32 %0, 1, 0, p;\n\t}"
-			: "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
-	return ok != 0;
-}
-
-// Polls of a bounded mbarrier wait before it gives up (about 1.6 s with
-// the suspend hint above).
-constexpr uint32_t kWaitPolls = 1u << 14;
+// Probes of a bounded wait before it gives up: each probe suspends the
+// thread at most for the hardware's time limit (of the order of a
+// microsecond), so a wait that never completes ends within about a second.
+constexpr uint32_t kWaitPolls = 1u << 20;
 
 // Wait for the mbarrier phase of the given parity, with an iteration limit:
 // on expiry the status word records ST_TIMEOUT and the caller goes on (its
@@ -378,24 +355,9 @@ constexpr uint32_t kWaitPolls = 1u << 14;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *status,
 		uint32_t polls = kWaitPolls)
 {
-#if CPIC_WAIT_MODE == 1
-	for(uint32_t it = 0; it < polls * 64u; it++)
-		if(mbar_try_wait_nohint(bar, parity))
-			return true;
-#elif CPIC_WAIT_MODE == 2
-	uint32_t ns = 32;
-	for(uint32_t it = 0; it < polls * 256u; it++)
-	{
-		if(mbar_test_wait(bar, parity))
-			return true;
-		__nanosleep(ns);
-		if(ns < 512) ns <<= 1;
-	}
-#else
 	for(uint32_t it = 0; it < polls; it++)
 		if(mbar_try_wait(bar, parity))
 			return true;
-#endif
 	set_status(status, ST_TIMEOUT);
 	return false;
 }

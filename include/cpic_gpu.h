@@ -166,9 +166,9 @@ CPIC_API uint32_t cpic_status_bits(cpic_ctx_t *ctx);
 
 /* No counterpart in the reference (it aborts instead of waiting).  Self-test
  * of the device-side bounded wait that every kernel of this library uses
- * on its shared-memory pipeline: one warp waits, with at most `polls` polls
- * (each may suspend the thread up to 100 us; at most the kernels' own limit
- * of 16384), on an mbarrier phase that never completes.  It is armed for
+ * on its shared-memory pipeline: one warp waits, with at most `polls` probes
+ * (each may suspend the thread for the hardware's time limit; at most the
+ * kernels' own limit of 2^20), on an mbarrier phase that never completes.  It is armed for
  * the bytes of a copy that is never issued, so nothing is in flight.
  * Returns CPIC_ETIMEOUT when the wait expired and the kernel returned, as it
  * must; the device stays usable afterwards. */

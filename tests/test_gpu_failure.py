@@ -64,7 +64,7 @@ def test_velocity_above_umax_returns_eumax(lib, precision):
 def test_bounded_wait_expires_and_device_stays_usable(lib):
     assert lib.cpic_selftest_wait(64) == -10     # CPIC_ETIMEOUT
     assert lib.cpic_selftest_wait(0) == -1
-    assert lib.cpic_selftest_wait(1 << 20) == -1
+    assert lib.cpic_selftest_wait(1 << 21) == -1
     case = cases.two_stream(n=4096)
     g = cases.make_gpu(case)
     o = cases.make_oracle(case)
