@@ -27,6 +27,10 @@
 #include "cpic_common.cuh"
 #include "cpic_bits.h"
 
+#ifndef CPIC_EARLY_RELEASE
+#define CPIC_EARLY_RELEASE 0
+#endif
+
 namespace cpic {
 
 // =================================================================== F64
@@ -835,10 +839,21 @@ k_push(const PushArgs a)
 		{
 			const int j = k * kPushThreads + threadIdx.x;
 			const bool valid = c0 + j < n;
+			if(valid)
+				rec[k] = F::template from_stage<kChunk>(buf, j, ids);
+#if CPIC_EARLY_RELEASE
+			// the last record is in registers: the buffer goes back to the
+			// producer before the last push, not after it
+			if(k == P - 1)
+			{
+				__syncwarp();
+				if(lane == 0)
+					mbar_arrive(&ebars[ci & 1]);
+			}
+#endif
 			dest[k] = -1;
 			if(valid)
 			{
-				rec[k] = F::template from_stage<kChunk>(buf, j, ids);
 				typename F::Out o = F::push(a, s, rec[k], tx0, ty0, Etile);
 				err |= o.err;
 				F::deposit(a, s, fsm, W, H, tx0, ty0, o);
@@ -849,10 +864,12 @@ k_push(const PushArgs a)
 			// results consumed after the stayer writes
 			rv[k] = warp_reserve_issue(T.app, dest[k] >= 0 && dest[k] != t, dest[k]);
 		}
+#if !CPIC_EARLY_RELEASE
 		// this warp is done with the staged chunk: release the buffer
 		__syncwarp();
 		if(lane == 0)
 			mbar_arrive(&ebars[ci & 1]);
+#endif
 		if(err) set_status(a.status, err);
 		// one shared-cursor reservation per warp for all its stayers
 		int nst = 0;
