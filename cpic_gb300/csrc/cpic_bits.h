@@ -13,6 +13,7 @@
 // (host and device), so a CPU test checks them against the FP64 operations
 // on edge cases and random values.
 #pragma once
+#include <climits>
 #include <cstdint>
 #include <cstring>
 
@@ -69,6 +70,37 @@ CPIC_HD bool floor_nonneg(double d, double &f, int &i)
 	f = from_bits(b & ~((1ull << sh) - 1ull));
 	i = (int) (m >> sh);
 	return true;
+}
+
+// The compares of the periodic wrap and of the velocity check, from the
+// bits (positive doubles order like their bit patterns read as integers).
+// Each gives the IEEE compare's result for every finite or infinite d; for a
+// NaN d the caller's result is NaN either way and is reported as such.
+
+// d >= L, for a finite L > 0
+CPIC_HD bool ge_pos(double d, double L)
+{
+	return (int64_t) to_bits(d) >= (int64_t) to_bits(L);
+}
+
+// d < 0.0 (false for -0.0)
+CPIC_HD bool lt_zero(double d)
+{
+	const int64_t b = (int64_t) to_bits(d);
+	return b < 0 && b != INT64_MIN;
+}
+
+// |d| > u, for a finite u >= 0 (false for a NaN d, as the IEEE compare)
+CPIC_HD bool abs_gt(double d, double u)
+{
+	const uint64_t a = to_bits(d) & 0x7fffffffffffffffull;
+	return a > to_bits(u) && a <= 0x7ff0000000000000ull;
+}
+
+// d is neither infinite nor NaN
+CPIC_HD bool is_finite(double d)
+{
+	return (to_bits(d) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
 }
 
 // mag / 2^k rounded to the nearest integer, ties to even, for k >= 0.

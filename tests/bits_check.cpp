@@ -2,6 +2,7 @@
 // operations it replaces, on edge cases and random values (CPU test driven
 // by tests/test_bits.py).  Prints the number of mismatches; 0 is a pass.
 #include <cfenv>
+#include <initializer_list>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -47,6 +48,22 @@ static void check_floor(double d)
 	}
 }
 
+static void check_cmp(double d, double L)
+{
+	checked++;
+	handled++;
+	bool ok = ge_pos(d, L) == (d >= L) || std::isnan(d);
+	ok = ok && (lt_zero(d) == (d < 0.0) || std::isnan(d));
+	ok = ok && abs_gt(d, L) == (std::fabs(d) > L);
+	ok = ok && is_finite(d) == (bool) std::isfinite(d);
+	if(!ok)
+	{
+		if(bad < 10)
+			std::printf("compare %.17g vs %.17g\n", d, L);
+		bad++;
+	}
+}
+
 int main()
 {
 	std::fesetround(FE_TONEAREST);
@@ -80,6 +97,15 @@ int main()
 	}
 	for(double d : {0.0, -0.0, 0.5, 1.0, 1.5, 2.0, 2047.9999999999998, 2048.0, 3.0e9, 2147483647.0})
 		check_floor(d);
+	const double Ls[] = {6.283185307179586, 1.0, 32.0, 0.5, 1e-3, 12.566370614359172};
+	for(double L : Ls)
+	{
+		for(double d : std::initializer_list<double>{0.0, -0.0, L, -L, std::nextafter(L, 0.0), std::nextafter(L, 1e300), 1e300,
+				-1e300, (double) INFINITY, (double) -INFINITY, (double) NAN, (double) -NAN, 1e-310, -1e-310})
+			check_cmp(d, L);
+		for(int t = 0; t < 200000; t++)
+			check_cmp(std::ldexp(u01(rng) * 2.0 - 1.0, (int) (rng() % 20) - 8) * L, L);
+	}
 	check_split(0.0, 30);
 	check_split(-0.0, 30);
 	std::printf("%ld mismatches of %ld handled (%ld checked)\n", bad, handled, checked);
