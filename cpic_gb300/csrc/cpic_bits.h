@@ -103,6 +103,28 @@ CPIC_HD bool is_finite(double d)
 	return (to_bits(d) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
 }
 
+// Division of a tile index by the number of tiles per row without a divide
+// instruction: q = t / n = (t * mul) >> sh (a 32 x 32 -> 64-bit product and
+// a shift), exact for every t < 2^30 and n in [1, 2^30).  With D = 2n,
+// c = ceil(log2 D) and mul = ceil(2^(31+c) / D) < 2^32: t * mul / 2^(30+c)
+// = 2t * mul / 2^(31+c) = t/n + 2t e / (D 2^(31+c)) with e = mul D -
+// 2^(31+c) < D <= 2^c, an excess below 1/n for 2t < 2^31.  For a power of
+// two n, mul = 2^31 and the result is t >> log2 n.
+CPIC_HD void div_init(uint32_t n, uint32_t &mul, int &sh)
+{
+	const uint64_t D = 2ull * n;
+	int c = 0;
+	while((1ull << c) < D)
+		c++;
+	mul = (uint32_t) (((1ull << (31 + c)) + D - 1) / D);
+	sh = 30 + c;
+}
+
+CPIC_HD uint32_t div_q(uint32_t t, uint32_t mul, int sh)
+{
+	return (uint32_t) (((uint64_t) t * mul) >> sh);
+}
+
 // mag / 2^k rounded to the nearest integer, ties to even, for k >= 0.
 CPIC_HD uint64_t rshift_rne(uint64_t mag, int k)
 {

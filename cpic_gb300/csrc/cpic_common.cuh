@@ -22,6 +22,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "cpic_bits.h"
 
 namespace cpic {
 
@@ -97,8 +98,13 @@ struct Grid {
 	int tx, ty;          // tile size in cells
 	int ntx, nty;        // tiles per dimension
 	int halo;            // deposit halo in cells
-	int lnx, lny;        // log2 of nx, ny (grids are powers of two)
-	int ltx, lty;        // log2 of tx, ty
+	int lcx;             // bits of x in a packed cell index (cy << lcx) + cx:
+	                     // ceil(log2 nx), so any nx decodes with a shift and
+	                     // a mask
+	int ltx, lty;        // log2 of tx, ty (tiles are powers of two)
+	uint32_t ntx_mul;    // t / ntx = (t * ntx_mul) >> ntx_sh for a tile
+	int ntx_sh;          // index t (bits::div_init)
+	int pow2;            // nx and ny are powers of two
 	double dx, dy, idx, idy, Lx, Ly;
 };
 
@@ -161,6 +167,39 @@ __device__ __forceinline__ int wrap2(int i, int n)
 	return i & (n - 1);
 }
 
+// Periodic wrap for any extent, i in [-n, 2n).
+__host__ __device__ __forceinline__ int wrapn(int i, int n)
+{
+	if(i < 0) i += n;
+	else if(i >= n) i -= n;
+	return i;
+}
+
+// Periodic wrap for any extent and any i (a loop: one or two compares for
+// i within one period of the grid).
+__host__ __device__ __forceinline__ int wrap_any(int i, int n)
+{
+	while(i < 0) i += n;
+	while(i >= n) i -= n;
+	return i;
+}
+
+// Periodic wrap for any extent and any i, with a division.
+__host__ __device__ __forceinline__ int wrap_mod(int i, int n)
+{
+	i %= n;
+	return i < 0 ? i + n : i;
+}
+
+// Row (ty) and column (tx) of tile index t, without a divide instruction
+// (bits::div_q: exact for t < 2^30; for a power-of-two ntx it is t >> log2
+// ntx).
+__device__ __forceinline__ void tile_rc(const Grid &g, int t, int &tx, int &ty)
+{
+	ty = (int) bits::div_q((uint32_t) t, g.ntx_mul, g.ntx_sh);
+	tx = t - ty * g.ntx;
+}
+
 __device__ __forceinline__ void set_status(uint32_t *st, uint32_t bit)
 {
 	atomicOr(st, bit);
@@ -169,7 +208,7 @@ __device__ __forceinline__ void set_status(uint32_t *st, uint32_t bit)
 // Tile index of a cell.
 __device__ __forceinline__ int tile_of(const Grid &g, int cx, int cy)
 {
-	return ((cy >> g.lty) << (g.lnx - g.ltx)) + (cx >> g.ltx);
+	return (cy >> g.lty) * g.ntx + (cx >> g.ltx);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -188,12 +227,12 @@ __device__ __forceinline__ void
 dep_global(long long *rho, const Grid &g, int cx, int cy,
 		long long w00, long long w01, long long w10, long long w11)
 {
-	int x0 = wrap2(cx, g.nx), y0 = wrap2(cy, g.ny);
-	int x1 = wrap2(x0 + 1, g.nx), y1 = wrap2(y0 + 1, g.ny);
-	red_global(&rho[((int64_t) y0 << g.lnx) + x0], w00);
-	red_global(&rho[((int64_t) y1 << g.lnx) + x0], w01);
-	red_global(&rho[((int64_t) y0 << g.lnx) + x1], w10);
-	red_global(&rho[((int64_t) y1 << g.lnx) + x1], w11);
+	int x0 = wrap_any(cx, g.nx), y0 = wrap_any(cy, g.ny);
+	int x1 = wrapn(x0 + 1, g.nx), y1 = wrapn(y0 + 1, g.ny);
+	red_global(&rho[(int64_t) y0 * g.nx + x0], w00);
+	red_global(&rho[(int64_t) y1 * g.nx + x0], w01);
+	red_global(&rho[(int64_t) y0 * g.nx + x1], w10);
+	red_global(&rho[(int64_t) y1 * g.nx + x1], w11);
 }
 
 // Two-word variant of dep_global (FP64 form: high and remainder words).
@@ -201,10 +240,10 @@ __device__ __forceinline__ void
 dep_global2(long long *rho, long long *rlo, const Grid &g, int cx, int cy,
 		const long long hi[4], const long long lo[4])
 {
-	int x0 = wrap2(cx, g.nx), y0 = wrap2(cy, g.ny);
-	int x1 = wrap2(x0 + 1, g.nx), y1 = wrap2(y0 + 1, g.ny);
-	int64_t n[4] = {((int64_t) y0 << g.lnx) + x0, ((int64_t) y1 << g.lnx) + x0,
-		((int64_t) y0 << g.lnx) + x1, ((int64_t) y1 << g.lnx) + x1};
+	int x0 = wrap_any(cx, g.nx), y0 = wrap_any(cy, g.ny);
+	int x1 = wrapn(x0 + 1, g.nx), y1 = wrapn(y0 + 1, g.ny);
+	int64_t n[4] = {(int64_t) y0 * g.nx + x0, (int64_t) y1 * g.nx + x0,
+		(int64_t) y0 * g.nx + x1, (int64_t) y1 * g.nx + x1};
 	for(int c = 0; c < 4; c++)
 	{
 		red_global(&rho[n[c]], hi[c]);
@@ -216,9 +255,9 @@ dep_global2(long long *rho, long long *rlo, const Grid &g, int cx, int cy,
 __device__ __forceinline__ int64_t
 frame_node(const Grid &g, int W, int H, int tx0, int ty0, int i)
 {
-	int gx = wrap2(tx0 - H + i % W, g.nx);
-	int gy = wrap2(ty0 - H + i / W, g.ny);
-	return ((int64_t) gy << g.lnx) + gx;
+	int gx = wrap_any(tx0 - H + i % W, g.nx);
+	int gy = wrap_any(ty0 - H + i / W, g.ny);
+	return (int64_t) gy * g.nx + gx;
 }
 
 // Split-phase variant: `issue` fires one atomic per distinct destination
@@ -442,7 +481,7 @@ cudaError_t launch_poisson_f64(const Grid &g, const long long *rho, double qinv,
 cudaError_t launch_push_mix(const PushArgs &a, int ntiles, size_t smem, int ppt, cudaStream_t s);
 // resident blocks per SM of the mixed fused kernel at this dynamic shared
 // memory, for a store with or without ids (0 on error)
-int push_mix_blocks_per_sm(size_t smem, bool ids, int ppt);
+int push_mix_blocks_per_sm(size_t smem, bool ids, int ppt, bool gp2);
 void launch_spill_mix(const SpillArgs &a, cudaStream_t s);
 void launch_E_mix(const Grid &g, const float *phi, float2 *E, cudaStream_t s);
 cudaError_t launch_poisson_mix(const Grid &g, const long long *rho, double qinv, const long long *rsum,

@@ -255,7 +255,7 @@ template <> struct TileOf<Mix> {
 	static __device__ __forceinline__ int get(const Grid &g, const Spill &S, int64_t k)
 	{
 		Mix::Rec r = Mix::from_spill(S, k, g);
-		return tile_of(g, r.cell % g.nx, r.cell / g.nx);
+		return tile_of(g, r.cell & ((1 << g.lcx) - 1), r.cell >> g.lcx);
 	}
 };
 
@@ -311,7 +311,7 @@ template <> struct RecTile<F64> {
 template <> struct RecTile<Mix> {
 	static __device__ __forceinline__ int get(const Grid &g, const Mix::Rec &r)
 	{
-		return tile_of(g, r.cell & (g.nx - 1), r.cell >> g.lnx);
+		return tile_of(g, r.cell & ((1 << g.lcx) - 1), r.cell >> g.lcx);
 	}
 };
 
@@ -439,31 +439,36 @@ k_rb_pass(const PushArgs in, const int32_t *kin, const PushArgs out, int32_t *ko
 	__shared__ int32_t wsum[kRbThreads / 32];
 	const Grid &g = out.g;
 	const int nt = g.ntx * g.nty;
-	const int ltxn = g.lnx - g.ltx, ntx = 1 << ltxn;
+	const int ntx = g.ntx;
 	const int64_t per = (n + gridDim.x - 1) / gridDim.x;
 	const int64_t lo = (int64_t) blockIdx.x * per, hi = min(n, lo + per);
 	if(lo >= hi) return;
+	// the tile of a key, and the row of a tile
+	auto key_tile = [&](int key) -> int { return key >= nt ? key - nt : key; };
+	auto row_of = [&](int tile) -> int {
+		return (int) bits::div_q((uint32_t) tile, g.ntx_mul, g.ntx_sh);
+	};
 	// local buckets: pass 1 all rows; pass 2 the rows [r0, r0 + R) of
 	// this range (its input is grouped by row), left movers first
-	const int r0 = kRows ? 0 : (kin[lo] & (nt - 1)) >> ltxn;
-	const int R = kRows ? nrow : ((kin[hi - 1] & (nt - 1)) >> ltxn) - r0 + 1;
+	const int r0 = kRows ? 0 : row_of(key_tile(kin[lo]));
+	const int R = kRows ? nrow : row_of(key_tile(kin[hi - 1])) - r0 + 1;
 	const int nbl = kRows ? nrow : 2 * R * ntx;
 	auto local = [&](int key) -> int {
-		const int tile = key & (nt - 1);
-		if(kRows) return tile >> ltxn;
-		return (key >= nt ? R * ntx : 0) + tile - (r0 << ltxn);
+		const int tile = key_tile(key);
+		if(kRows) return row_of(tile);
+		return (key >= nt ? R * ntx : 0) + tile - r0 * ntx;
 	};
 	auto global = [&](int l) -> int {
 		if(kRows) return l;
 		const int right = l >= R * ntx;
-		return (right ? nt : 0) + (r0 << ltxn) + l - (right ? R * ntx : 0);
+		return (right ? nt : 0) + r0 * ntx + l - (right ? R * ntx : 0);
 	};
 	if(nbl > kRbMaxLocal)
 	{
 		for(int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
 		{
 			const int key = kin[i];
-			const int gb = kRows ? (key & (nt - 1)) >> ltxn : key;
+			const int gb = kRows ? row_of(key_tile(key)) : key;
 			if(key < 0 || key >= 2 * nt) { set_status(out.status, ST_RANGE); continue; }
 			const int64_t dst = (int64_t) atomicAdd(&cursor[gb], 1ULL);
 			if(dst < 0 || dst >= ncap_out) { set_status(out.status, ST_RANGE); continue; }
@@ -1057,14 +1062,14 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	{
 		// pass 1: by row of tiles into a temporary store; pass 2: by
 		// (direction, tile) into the new layout
-		const int ltxn = c->g.lnx - c->g.ltx;          // log2 tiles per row
-		const int nrow = nt >> ltxn;
+		const int ntx = c->g.ntx;                      // tiles per row
+		const int nrow = c->g.nty;
 		std::vector<unsigned long long> rowcur(nrow);
 		unsigned long long acc = 0;
 		for(int r = 0; r < nrow; r++)
 		{
 			rowcur[r] = acc;
-			for(int t = r << ltxn; t < (r + 1) << ltxn; t++) acc += (unsigned long long) hc[t];
+			for(int t = r * ntx; t < (r + 1) * ntx; t++) acc += (unsigned long long) hc[t];
 		}
 		int r = alloc_store(c, tmp2, nstage, false);
 		if(r) return r;
@@ -1170,7 +1175,7 @@ static bool tile_order_pays(const cpic_ctx *c, size_t smem)
 			|| cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
 		return true;
 	const int per_sm = c->precision == CPIC_MIXED
-		? push_mix_blocks_per_sm(smem, c->p.track_ids != 0, c->ppt)
+		? push_mix_blocks_per_sm(smem, c->p.track_ids != 0, c->ppt, c->g.pow2 != 0)
 		: push_f64_blocks_per_sm(smem, c->ppt);
 	return per_sm <= 0 || (int64_t) c->ntiles > (int64_t) per_sm * nsm;
 }
@@ -1303,8 +1308,9 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 {
 	if(!p || !out) return CPIC_EINVAL;
 	*out = nullptr;
-	if(!pow2(p->nx) || !pow2(p->ny) || p->nx < 4 || p->ny < 4 || p->nx > (1 << 14)
-			|| p->ny > (1 << 14))
+	// any grid from 4 x 4 to 16384 x 16384 cells (the reference's FFTW
+	// solver takes any nx, ny: solver.c:246-330)
+	if(p->nx < 4 || p->ny < 4 || p->nx > (1 << 14) || p->ny > (1 << 14))
 		return CPIC_EINVAL;
 	if(!(p->Lx > 0) || !(p->Ly > 0) || !(p->dt > 0) || !(p->e0 > 0))
 		return CPIC_EINVAL;
@@ -1336,16 +1342,18 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	int T = p->tile_x;
 	if(T <= 0)
 	{
-		// autotune default: the largest tile with at least 2048 tiles,
-		// else the largest tile giving at least 64 tiles, else 4 cells
-		T = 4;
-		for(int cand = 64; cand >= 4; cand >>= 1)
+		// default: the largest tile with at least 2048 tiles, else the
+		// largest tile giving at least 64 tiles, else the largest power of
+		// two up to 32 dividing both sides (1 for an odd side)
+		T = 0;
+		for(int cand = 64; cand >= 4 && !T; cand >>= 1)
 			if(p->nx % cand == 0 && p->ny % cand == 0
-					&& (p->nx / cand) * (p->ny / cand) >= 2048) { T = cand; break; }
-		if(T == 4)
-			for(int cand = 32; cand >= 4; cand >>= 1)
-				if(p->nx % cand == 0 && p->ny % cand == 0
-						&& (p->nx / cand) * (p->ny / cand) >= 64) { T = cand; break; }
+					&& (p->nx / cand) * (p->ny / cand) >= 2048) T = cand;
+		for(int cand = 32; cand >= 4 && !T; cand >>= 1)
+			if(p->nx % cand == 0 && p->ny % cand == 0
+					&& (p->nx / cand) * (p->ny / cand) >= 64) T = cand;
+		for(int cand = 32; cand >= 1 && !T; cand >>= 1)
+			if(p->nx % cand == 0 && p->ny % cand == 0) T = cand;
 	}
 	int TY = p->tile_y > 0 ? p->tile_y : T;
 	if(!pow2(T) || !pow2(TY) || p->nx % T || p->ny % TY || T != TY)
@@ -1362,8 +1370,10 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	g.tx = T; g.ty = TY;
 	g.ntx = g.nx / T; g.nty = g.ny / TY;
 	g.halo = p->halo > 0 ? p->halo : 2;
-	g.lnx = ilog2(g.nx); g.lny = ilog2(g.ny);
+	g.lcx = ilog2(g.nx);
 	g.ltx = ilog2(T); g.lty = ilog2(TY);
+	bits::div_init((uint32_t) g.ntx, g.ntx_mul, g.ntx_sh);
+	g.pow2 = pow2(g.nx) && pow2(g.ny);
 	c->ntiles = g.ntx * g.nty;
 	// the main stream at the highest priority: the field solve's blocks go
 	// ahead of the fix-up blocks still waiting on the low-priority side
@@ -1399,8 +1409,8 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 		AL(c->Ex64, (ng + 3 * (int64_t) g.nx) * sizeof(double));
 		AL(c->Ey64, (ng + 3 * (int64_t) g.nx) * sizeof(double));
 		AL(c->spec64, ng / g.nx * nh * sizeof(double2));
-		AL(c->twx64, g.nx / 2 * sizeof(double2));
-		AL(c->twy64, g.ny / 2 * sizeof(double2));
+		AL(c->twx64, g.nx * sizeof(double2));
+		AL(c->twy64, g.ny * sizeof(double2));
 		cudaMemset(c->Ex64, 0, (ng + 3 * (int64_t) g.nx) * sizeof(double));
 		cudaMemset(c->Ey64, 0, (ng + 3 * (int64_t) g.nx) * sizeof(double));
 	}
@@ -1409,8 +1419,8 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 		AL(c->phi32, ng * sizeof(float));
 		AL(c->E32, ng * sizeof(float2));
 		AL(c->spec32, ng / g.nx * nh * sizeof(float2));
-		AL(c->twx32, g.nx / 2 * sizeof(float2));
-		AL(c->twy32, g.ny / 2 * sizeof(float2));
+		AL(c->twx32, g.nx * sizeof(float2));
+		AL(c->twy32, g.ny * sizeof(float2));
 		cudaMemset(c->E32, 0, ng * sizeof(float2));
 	}
 #undef AL
@@ -1419,7 +1429,8 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	cudaMemset(c->status, 0, sizeof(uint32_t));
 	{
 		// Green's function cosines as MFT_init computes them
-		// (solver.c:257-278) and FFT twiddles exp(-2 pi i k / n).
+		// (solver.c:257-278) and FFT twiddles exp(-2 pi i k / n), k < n
+		// (a power-of-two transform reads the first half).
 		std::vector<double> cx(g.nx), cy(g.ny);
 		double ccx = 2.0 * M_PI / g.nx, ccy = 2.0 * M_PI / g.ny;
 		for(int i = 0; i < g.nx; i++) cx[i] = cos(ccx * i);
@@ -1429,19 +1440,19 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 		for(int dim = 0; dim < 2; dim++)
 		{
 			int n = dim == 0 ? g.nx : g.ny;
-			std::vector<double2> tw(n / 2);
-			std::vector<float2> tf(n / 2);
-			for(int k = 0; k < n / 2; k++)
+			std::vector<double2> tw(n);
+			std::vector<float2> tf(n);
+			for(int k = 0; k < n; k++)
 			{
 				double a = -2.0 * M_PI * k / n;
 				tw[k] = make_double2(cos(a), sin(a));
 				tf[k] = make_float2((float) cos(a), (float) sin(a));
 			}
 			if(c->precision == CPIC_FP64)
-				cudaMemcpy(dim == 0 ? c->twx64 : c->twy64, tw.data(), n / 2 * sizeof(double2),
+				cudaMemcpy(dim == 0 ? c->twx64 : c->twy64, tw.data(), n * sizeof(double2),
 						cudaMemcpyHostToDevice);
 			else
-				cudaMemcpy(dim == 0 ? c->twx32 : c->twy32, tf.data(), n / 2 * sizeof(float2),
+				cudaMemcpy(dim == 0 ? c->twx32 : c->twy32, tf.data(), n * sizeof(float2),
 						cudaMemcpyHostToDevice);
 		}
 	}
@@ -1634,8 +1645,8 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 		int H = std::max(hmin, std::min((int) ceil(1.2 * D) + 1, c->g.tx));
 		if(c->precision == CPIC_MIXED)
 		{
-			int target = push_mix_blocks_per_sm(push_smem_h(c, hmin), c->p.track_ids != 0, c->ppt);
-			while(H > hmin && push_mix_blocks_per_sm(push_smem_h(c, H), c->p.track_ids != 0, c->ppt)
+			int target = push_mix_blocks_per_sm(push_smem_h(c, hmin), c->p.track_ids != 0, c->ppt, c->g.pow2 != 0);
+			while(H > hmin && push_mix_blocks_per_sm(push_smem_h(c, H), c->p.track_ids != 0, c->ppt, c->g.pow2 != 0)
 					< target)
 				H--;
 		}
@@ -2100,7 +2111,7 @@ CPIC_API int cpic_layout_stats(const cpic_ctx_t *c, int64_t *out)
 	if(c->nspecies > 0)
 	{
 		if(c->precision == CPIC_MIXED)
-			out[3] = push_mix_blocks_per_sm(push_smem(c), c->p.track_ids != 0, c->ppt);
+			out[3] = push_mix_blocks_per_sm(push_smem(c), c->p.track_ids != 0, c->ppt, c->g.pow2 != 0);
 		else
 			out[3] = push_f64_blocks_per_sm(push_smem(c), c->ppt);
 	}
@@ -2441,7 +2452,11 @@ static int autotune(const cpic_params_t *p, int64_t n, double v0, double vth, bo
 	double q = -p->Lx * p->Ly / (double) n;
 	int32_t best = 0, best_p = 0;
 	double best_ms = INFINITY;
+	// tiles of 1 and 2 cells only for grids no larger tile divides
+	bool big = false;
 	for(int32_t T = 4; T <= 64; T *= 2)
+		big = big || (p->nx % T == 0 && p->ny % T == 0 && (p->nx / T) * (p->ny / T) >= 4);
+	for(int32_t T = big ? 4 : 1; T <= 64; T *= 2)
 	{
 		if(p->nx % T || p->ny % T || (p->nx / T) * (p->ny / T) < 4) continue;
 		for(int P : kPPTChoices)

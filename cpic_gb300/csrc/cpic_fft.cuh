@@ -1,13 +1,14 @@
-// cpic_fft.cuh -- periodic FFT Poisson solver for power-of-two grids,
-// templated on the real type (double for the FP64 form, float for the
-// mixed form).
+// cpic_fft.cuh -- periodic FFT Poisson solver for any grid (radix-4/2
+// passes for power-of-two sides, mixed-radix passes otherwise), templated
+// on the real type (double for the FP64 form, float for the mixed form).
 //
 // Replaces MFT_solve (src/solver.c:465-509): phi = IFFT(G * FFT(rho)) / (nx
 // ny) with G(kx,ky) = 1 / (2 (cos(2 pi kx/nx) + cos(2 pi ky/ny)) - 4) and
 // G(0,0) = 0 (solver.c:269-280).  Three kernels, all working in shared
-// memory with Stockham radix-4 passes (self-sorting, no bit reversal):
+// memory with Stockham passes (self-sorting, no bit reversal):
 //   rows_fwd : two real rows packed as one complex row, FFT along x, split
-//              into the two half spectra (nx/2+1 bins each);
+//              into the two half spectra (nx/2+1 bins each; the last row
+//              of an odd ny alone);
 //   cols     : a block of spectrum columns, FFT along y, multiply by G,
 //              inverse FFT along y (the Green's function never leaves
 //              shared memory);
@@ -115,6 +116,70 @@ __device__ C *fft_smem(C *a, C *b, int n, int log2n, int nb, int sign, const C *
 	return a;
 }
 
+// Any n >= 2 (the power-of-two passes above when n is one): mixed-radix
+// Stockham passes over the prime factors of n (4s first, then 2, then the
+// odd primes in increasing order), each pass computing every output
+// directly from its r inputs.  A pass of radix r after sub-transforms of
+// length Ns (the product of the radices before it) writes
+//   y[(j - k) r + k + p Ns] = sum_q x[j + q n/r] exp(sign 2 pi i q (k + p Ns) / (r Ns))
+// for j < n/r, k = j mod Ns, p < r: the twiddle and the r-point DFT in
+// one exponent, read from the full table tw[m] = exp(-2 pi i m / n), m < n
+// (conjugated for the inverse).  O(n r) work per pass: a length with a
+// large prime factor transforms correctly but slowly.
+template <typename C>
+__device__ C *fft_smem_any(C *a, C *b, int n, int nb, int sign, const C *tw)
+{
+	int rem = n, Ns = 1;
+	while(rem > 1)
+	{
+		int r;
+		if(rem % 4 == 0) r = 4;
+		else if(rem % 2 == 0) r = 2;
+		else
+		{
+			r = 3;
+			while(rem % r) r += 2;
+		}
+		const int m = n / r;                 // outputs per output digit p
+		const int step0 = n / (r * Ns);      // table stride of one unit of k + p Ns
+		const int total = n * nb;
+		for(int idx = threadIdx.x; idx < total; idx += blockDim.x)
+		{
+			const int seq = idx / n, o = idx - seq * n;
+			const int p = o / m, j = o - p * m;
+			const int k = j % Ns;
+			const C *x = a + (size_t) seq * n;
+			const int step = (k + p * Ns) * step0;   // < n
+			C acc = x[j];
+			int t = 0;
+			for(int q = 1; q < r; q++)
+			{
+				t += step;
+				if(t >= n) t -= n;
+				C w = tw[t];
+				if(sign > 0) w.y = -w.y;
+				acc = cadd(acc, cmul(x[j + q * m], w));
+			}
+			b[(size_t) seq * n + (j - k) * r + k + p * Ns] = acc;
+		}
+		__syncthreads();
+		C *t = a; a = b; b = t;
+		Ns *= r;
+		rem /= r;
+	}
+	return a;
+}
+
+// The transform of fft_smem for a power-of-two n (log2n its exponent), of
+// fft_smem_any otherwise.
+template <typename C>
+__device__ __forceinline__ C *fft_any(C *a, C *b, int n, int log2n, int nb, int sign, const C *tw)
+{
+	if((1 << log2n) == n)
+		return fft_smem<C>(a, b, n, log2n, nb, sign, tw);
+	return fft_smem_any<C>(a, b, n, nb, sign, tw);
+}
+
 // The kernels below are static: the FP64 units (built without FMA
 // contraction) and the mixed and adjoint units (built with it) each get their
 // own copy, so a launch always runs the device code of the unit that makes
@@ -141,27 +206,28 @@ static __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *r
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + nx;
 	int r0 = 2 * blockIdx.x;
+	const bool two = r0 + 1 < ny;            // an odd ny leaves the last row alone
 	int nh = nx / 2 + 1;
 	double m = rsum ? (double) *rsum * qinv / ((double) nx * (double) ny) : mean0;
 	for(int i = threadIdx.x; i < nx; i += blockDim.x)
 	{
 		int64_t ia = (int64_t) r0 * nx + i, ib = (int64_t) (r0 + 1) * nx + i;
 		double va = (double) rho[ia] * qinv - m;
-		double vb = (double) rho[ib] * qinv - m;
+		double vb = two ? (double) rho[ib] * qinv - m : 0.0;
 		if(rho_lo)
 		{
 			va += (double) rho_lo[ia] * qinv_lo;
-			vb += (double) rho_lo[ib] * qinv_lo;
+			if(two) vb += (double) rho_lo[ib] * qinv_lo;
 		}
 		C z; z.x = (T) va; z.y = (T) vb;
 		a[i] = z;
 	}
 	__syncthreads();
-	C *Z = fft_smem<C>(a, b, nx, log2nx, 1, -1, tw);
+	C *Z = fft_any<C>(a, b, nx, log2nx, 1, -1, tw);
 	for(int k = threadIdx.x; k < nh; k += blockDim.x)
 	{
 		C p = Z[k];
-		C q = Z[(nx - k) & (nx - 1)];
+		C q = Z[k == 0 ? 0 : nx - k];
 		q.y = -q.y;                          // conj(Z[-k])
 		C A, B;
 		A.x = (p.x + q.x) * (T) 0.5;
@@ -170,7 +236,7 @@ static __global__ void k_rows_fwd(int nx, int log2nx, int ny, const long long *r
 		B.x = (p.y - q.y) * (T) 0.5;
 		B.y = -(p.x - q.x) * (T) 0.5;
 		spec[(int64_t) r0 * nh + k] = A;
-		spec[(int64_t) (r0 + 1) * nh + k] = B;
+		if(two) spec[(int64_t) (r0 + 1) * nh + k] = B;
 	}
 }
 
@@ -218,7 +284,7 @@ static __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>
 		a[c * ny + row] = spec[(int64_t) row * nh + c0 + c];
 	}
 	__syncthreads();
-	C *X = fft_smem<C>(a, b, ny, log2ny, ncol, -1, tw);
+	C *X = fft_any<C>(a, b, ny, log2ny, ncol, -1, tw);
 	if(Gt)
 	{
 		const T *Gc = Gt + (size_t) c0 * ny;    // columns are contiguous
@@ -235,7 +301,7 @@ static __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>
 	{
 		for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
 		{
-			int c = idx >> log2ny, row = idx - (c << log2ny);
+			int c = idx / ny, row = idx - c * ny;
 			int kx = c0 + c;
 			double G = (kx == 0 && row == 0) ? 0.0 : 1.0 / (2.0 * (cosx[kx] + cosy[row]) - 4.0);
 			C v = X[idx];
@@ -246,7 +312,7 @@ static __global__ void k_cols(int nx, int ny, int log2ny, int cb, typename Cx<T>
 	}
 	__syncthreads();
 	C *Y = (X == a) ? b : a;
-	C *R = fft_smem<C>(X, Y, ny, log2ny, ncol, +1, tw);
+	C *R = fft_any<C>(X, Y, ny, log2ny, ncol, +1, tw);
 	for(int idx = threadIdx.x; idx < ncol * ny; idx += blockDim.x)
 	{
 		int row = lg >= 0 ? idx >> lg : idx / ncol, c = idx - row * ncol;
@@ -264,12 +330,15 @@ static __global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + nx;
 	int r0 = 2 * blockIdx.x;
+	const bool two = r0 + 1 < ny;            // an odd ny leaves the last row alone
 	int nh = nx / 2 + 1;
 	for(int k = threadIdx.x; k < nh; k += blockDim.x)
 	{
 		C A = spec[(int64_t) r0 * nh + k];
-		C B = spec[(int64_t) (r0 + 1) * nh + k];
-		if(k == 0 || k == nx / 2)
+		C B;
+		if(two) B = spec[(int64_t) (r0 + 1) * nh + k];
+		else { B.x = (T) 0; B.y = (T) 0; }
+		if(k == 0 || 2 * k == nx)
 		{
 			// c2r uses only the real part of the DC and Nyquist bins
 			C y; y.x = A.x; y.y = B.x;
@@ -285,41 +354,42 @@ static __global__ void k_rows_inv(int nx, int log2nx, int ny, const typename Cx<
 		}
 	}
 	__syncthreads();
-	C *Y = fft_smem<C>(a, b, nx, log2nx, 1, +1, tw);
+	C *Y = fft_any<C>(a, b, nx, log2nx, 1, +1, tw);
 	T N = (T) ((double) nx * (double) ny);
 	for(int i = threadIdx.x; i < nx; i += blockDim.x)
 	{
 		C v = Y[i];
 		phi[(int64_t) r0 * nx + i] = v.x / N;
-		phi[(int64_t) (r0 + 1) * nx + i] = v.y / N;
+		if(two) phi[(int64_t) (r0 + 1) * nx + i] = v.y / N;
 	}
 }
 
 // Real-valued input (ny x nx of T) -> spec, otherwise as k_rows_fwd.  Used
 // by the adjoint, whose source term (rho-bar) is not a charge sum.
 template <typename T>
-static __global__ void k_rows_fwd_real(int nx, int log2nx, const T *in, typename Cx<T>::t *spec,
-		const typename Cx<T>::t *tw)
+static __global__ void k_rows_fwd_real(int nx, int log2nx, int ny, const T *in,
+		typename Cx<T>::t *spec, const typename Cx<T>::t *tw)
 {
 	typedef typename Cx<T>::t C;
 	extern __shared__ unsigned char smem_raw[];
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + nx;
 	int r0 = 2 * blockIdx.x;
+	const bool two = r0 + 1 < ny;
 	int nh = nx / 2 + 1;
 	for(int i = threadIdx.x; i < nx; i += blockDim.x)
 	{
 		C z;
 		z.x = in[(int64_t) r0 * nx + i];
-		z.y = in[(int64_t) (r0 + 1) * nx + i];
+		z.y = two ? in[(int64_t) (r0 + 1) * nx + i] : (T) 0;
 		a[i] = z;
 	}
 	__syncthreads();
-	C *Z = fft_smem<C>(a, b, nx, log2nx, 1, -1, tw);
+	C *Z = fft_any<C>(a, b, nx, log2nx, 1, -1, tw);
 	for(int k = threadIdx.x; k < nh; k += blockDim.x)
 	{
 		C p = Z[k];
-		C q = Z[(nx - k) & (nx - 1)];
+		C q = Z[k == 0 ? 0 : nx - k];
 		q.y = -q.y;
 		C A, B;
 		A.x = (p.x + q.x) * (T) 0.5;
@@ -327,7 +397,7 @@ static __global__ void k_rows_fwd_real(int nx, int log2nx, const T *in, typename
 		B.x = (p.y - q.y) * (T) 0.5;
 		B.y = -(p.x - q.x) * (T) 0.5;
 		spec[(int64_t) r0 * nh + k] = A;
-		spec[(int64_t) (r0 + 1) * nh + k] = B;
+		if(two) spec[(int64_t) (r0 + 1) * nh + k] = B;
 	}
 }
 
@@ -344,7 +414,7 @@ static void poisson_launch(const Grid &g, const long long *rho, double qinv, con
 	while((1 << log2ny) < g.ny) log2ny++;
 	int rthreads = g.nx / 2 < 512 ? (g.nx / 2 < 32 ? 32 : g.nx / 2) : 512;
 	size_t rsm = 2 * (size_t) g.nx * sizeof(C);
-	k_rows_fwd<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, rho, qinv, mean, spec, twx,
+	k_rows_fwd<T><<<(g.ny + 1) / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, rho, qinv, mean, spec, twx,
 			rho_lo, qinv_lo, mean0);
 	int nh = g.nx / 2 + 1;
 	// columns per block: up to 64 KB of shared memory (two buffers), so
@@ -356,7 +426,7 @@ static void poisson_launch(const Grid &g, const long long *rho, double qinv, con
 	int cthreads = 512;
 	k_cols<T><<<(nh + cb - 1) / cb, cthreads, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy,
 			Gt);
-	k_rows_inv<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, phi);
+	k_rows_inv<T><<<(g.ny + 1) / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, phi);
 }
 
 // out = IFFT(G FFT(in)) / (nx ny) for a real ny x nx input: the same linear
@@ -372,7 +442,7 @@ static void poisson_launch_real(const Grid &g, const T *in, typename Cx<T>::t *s
 	while((1 << log2ny) < g.ny) log2ny++;
 	int rthreads = g.nx / 2 < 512 ? (g.nx / 2 < 32 ? 32 : g.nx / 2) : 512;
 	size_t rsm = 2 * (size_t) g.nx * sizeof(C);
-	k_rows_fwd_real<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, in, spec, twx);
+	k_rows_fwd_real<T><<<(g.ny + 1) / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, in, spec, twx);
 	int nh = g.nx / 2 + 1;
 	int cb = (int) ((64 * 1024) / (2 * (size_t) g.ny * sizeof(C)));
 	if(cb < 1) cb = 1;
@@ -380,7 +450,7 @@ static void poisson_launch_real(const Grid &g, const T *in, typename Cx<T>::t *s
 	size_t csm = 2 * (size_t) cb * g.ny * sizeof(C);
 	k_cols<T><<<(nh + cb - 1) / cb, 512, csm, s>>>(g.nx, g.ny, log2ny, cb, spec, twy, cosx, cosy,
 			nullptr);
-	k_rows_inv<T><<<g.ny / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, out);
+	k_rows_inv<T><<<(g.ny + 1) / 2, rthreads, rsm, s>>>(g.nx, log2nx, g.ny, spec, twx, out);
 }
 
 } // namespace cpic

@@ -1,6 +1,7 @@
 // cpic_fp64.cu -- FP64 ("plain") form of the step.  Compiled with
 // --fmad=false so that every FP64 expression rounds exactly as the
 // reference's C code does (no FMA contraction).
+#include <algorithm>
 #include "cpic_common.cuh"
 #include "cpic_push.cuh"
 #include "cpic_fft.cuh"
@@ -12,29 +13,30 @@ namespace cpic {
 // phi ghosts (src/comm_field.c:140-201), which equals periodic indexing.
 __global__ void k_E_f64(Grid g, const double *phi, double *Ex, double *Ey)
 {
-	int64_t total = (int64_t) (g.ny + 1) * g.nx;
 	double dx2 = 2 * g.dx, dy2 = 2 * g.dy;
-	for(int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
-			i += (int64_t) gridDim.x * blockDim.x)
+	// rows 0..ny over blockIdx.y (row ny is the south ghost: row 0 again)
+	for(int iy = blockIdx.y; iy <= g.ny; iy += gridDim.y)
 	{
-		int iy = (int) (i >> g.lnx), ix = (int) i & (g.nx - 1);
-		// rows 0..ny (row ny is the south ghost: row 0 again)
 		int y0 = iy - 1 < 0 ? g.ny - 1 : iy - 1;
-		int y1 = (iy + 1) & (g.ny - 1);
-		int yc = iy & (g.ny - 1);
-		int x0 = (ix - 1) & (g.nx - 1);
-		int x1 = (ix + 1) & (g.nx - 1);
-		Ey[i] = (phi[(int64_t) y0 * g.nx + ix] - phi[(int64_t) y1 * g.nx + ix]) / dy2;
-		Ex[i] = (phi[(int64_t) yc * g.nx + x0] - phi[(int64_t) yc * g.nx + x1]) / dx2;
+		int y1 = iy + 1 >= g.ny ? iy + 1 - g.ny : iy + 1;
+		int yc = iy >= g.ny ? iy - g.ny : iy;
+		for(int ix = blockIdx.x * blockDim.x + threadIdx.x; ix < g.nx;
+				ix += gridDim.x * blockDim.x)
+		{
+			int x0 = ix == 0 ? g.nx - 1 : ix - 1;
+			int x1 = ix + 1 == g.nx ? 0 : ix + 1;
+			int64_t i = (int64_t) iy * g.nx + ix;
+			Ey[i] = (phi[(int64_t) y0 * g.nx + ix] - phi[(int64_t) y1 * g.nx + ix]) / dy2;
+			Ex[i] = (phi[(int64_t) yc * g.nx + x0] - phi[(int64_t) yc * g.nx + x1]) / dx2;
+		}
 	}
 }
 
 void launch_E_f64(const Grid &g, const double *phi, double *Ex, double *Ey, cudaStream_t s)
 {
-	int64_t total = (int64_t) (g.ny + 1) * g.nx;
-	int blocks = (int) ((total + 255) / 256);
-	if(blocks > 4096) blocks = 4096;
-	k_E_f64<<<blocks, 256, 0, s>>>(g, phi, Ex, Ey);
+	dim3 grid((g.nx + 255) / 256, 1);
+	grid.y = (unsigned) std::min(g.ny + 1, std::max(1, 4096 / (int) grid.x));
+	k_E_f64<<<grid, 256, 0, s>>>(g, phi, Ex, Ey);
 }
 
 // E at every particle (interpolate_f2p_E), written by particle id.  One

@@ -167,6 +167,7 @@ struct F64 {
 
 	// One particle.  tx0/ty0: origin of the tile it is processed in.
 	// deposit_only: keep the state, only compute the deposit (pre-step).
+	template <bool GP2 = true>
 	static __device__ __forceinline__ Out push(const PushArgs &a, int s, Rec &r,
 			int tx0, int ty0, const void *)
 	{
@@ -300,8 +301,8 @@ struct F64 {
 				int x = xs[c], y = ys[c];
 				if(x < 0 || x >= g.nx || y < 0 || y > g.ny) continue;
 				if(y == g.ny) y = 0;
-				red_global(&a.rho[((int64_t) y << g.lnx) + x], o.w[c]);
-				red_global(&a.rho_lo[((int64_t) y << g.lnx) + x], o.wl[c]);
+				red_global(&a.rho[(int64_t) y * g.nx + x], o.w[c]);
+				red_global(&a.rho_lo[(int64_t) y * g.nx + x], o.wl[c]);
 			}
 			return;
 		}
@@ -474,6 +475,7 @@ struct Mix {
 
 	// Etile: (T+1) x (T+1) shared tile of E at the tile's nodes, or null
 	// for the global field (spill records).
+	template <bool GP2 = true>
 	static __device__ __forceinline__ Out push(const PushArgs &a, int s, Rec &r,
 			int tx0, int ty0, const void *Etile)
 	{
@@ -486,7 +488,7 @@ struct Mix {
 		// function separately, and the compiler may not contract or
 		// reassociate differently in the two, so a particle gets the same
 		// result on either path.
-		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
+		int cx = r.cell & ((1 << g.lcx) - 1), cy = r.cell >> g.lcx;
 		float ox = r.ox, oy = r.oy;
 		float dxo = __fsub_rn(1.0f, ox), dyo = __fsub_rn(1.0f, oy);
 		float w00 = __fmul_rn(dxo, dyo), w01 = __fmul_rn(dxo, oy);
@@ -504,11 +506,11 @@ struct Mix {
 		{
 			// spill records, and particles kept outside their tile when
 			// their destination and the spill list were both full
-			int x1 = wrap2(cx + 1, g.nx), y1 = wrap2(cy + 1, g.ny);
-			e00 = a.E32[((int64_t) cy << g.lnx) + cx];
-			e01 = a.E32[((int64_t) y1 << g.lnx) + cx];
-			e10 = a.E32[((int64_t) cy << g.lnx) + x1];
-			e11 = a.E32[((int64_t) y1 << g.lnx) + x1];
+			int x1 = wrapn(cx + 1, g.nx), y1 = wrapn(cy + 1, g.ny);
+			e00 = a.E32[(int64_t) cy * g.nx + cx];
+			e01 = a.E32[(int64_t) y1 * g.nx + cx];
+			e10 = a.E32[(int64_t) cy * g.nx + x1];
+			e11 = a.E32[(int64_t) y1 * g.nx + x1];
 		}
 		float ex = __fmaf_rn(w11, e11.x, __fmaf_rn(w10, e10.x, __fmaf_rn(w01, e01.x,
 				__fmul_rn(w00, e00.x))));
@@ -542,8 +544,21 @@ struct Mix {
 			if(ox >= 1.0f) { ox = __fsub_rn(ox, 1.0f); sx += 1; }
 			if(oy >= 1.0f) { oy = __fsub_rn(oy, 1.0f); sy += 1; }
 		}
-		int ncx = wrap2(cx + sx, g.nx), ncy = wrap2(cy + sy, g.ny);
-		r.cell = (ncy << g.lnx) + ncx;
+		// the new cell, wrapped: a mask on a power-of-two grid; else a
+		// compare, and a division only for a move beyond one period (a
+		// particle over the velocity limit, already flagged)
+		int ncx = cx + sx, ncy = cy + sy;
+		if(GP2)
+		{
+			ncx = wrap2(ncx, g.nx);
+			ncy = wrap2(ncy, g.ny);
+		}
+		else
+		{
+			if((unsigned) ncx >= (unsigned) g.nx) ncx = wrap_mod(ncx, g.nx);
+			if((unsigned) ncy >= (unsigned) g.ny) ncy = wrap_mod(ncy, g.ny);
+		}
+		r.cell = (ncy << g.lcx) + ncx;
 		r.ox = ox; r.oy = oy; r.ux = ux; r.uy = uy;
 
 		dxo = __fsub_rn(1.0f, ox); dyo = __fsub_rn(1.0f, oy);
@@ -666,8 +681,8 @@ struct Mix {
 		for(int i = threadIdx.x; i < WE * (g.ty + 1); i += blockDim.x)
 		{
 			int lx = i % WE, ly = i / WE;
-			int gx = wrap2(tx0 + lx, g.nx), gy = wrap2(ty0 + ly, g.ny);
-			Et[i] = a.E32[((int64_t) gy << g.lnx) + gx];
+			int gx = wrapn(tx0 + lx, g.nx), gy = wrapn(ty0 + ly, g.ny);
+			Et[i] = a.E32[(int64_t) gy * g.nx + gx];
 		}
 		return Et;
 	}
@@ -678,11 +693,11 @@ struct Mix {
 		double px = S.cell_units ? S.x[k] : S.x[k] * g.idx;
 		double py = S.cell_units ? S.y[k] : S.y[k] * g.idy;
 		double fx = floor(px), fy = floor(py);
-		int cx = wrap2((int) fx, g.nx), cy = wrap2((int) fy, g.ny);
+		int cx = wrap_mod((int) fx, g.nx), cy = wrap_mod((int) fy, g.ny);
 		float ox = (float) (px - fx), oy = (float) (py - fy);
-		if(ox >= 1.0f) { ox = 0.0f; cx = wrap2(cx + 1, g.nx); }
-		if(oy >= 1.0f) { oy = 0.0f; cy = wrap2(cy + 1, g.ny); }
-		r.cell = (cy << g.lnx) + cx;
+		if(ox >= 1.0f) { ox = 0.0f; cx = wrapn(cx + 1, g.nx); }
+		if(oy >= 1.0f) { oy = 0.0f; cy = wrapn(cy + 1, g.ny); }
+		r.cell = (cy << g.lcx) + cx;
 		r.ox = ox; r.oy = oy;
 		r.ux = (float) S.ux[k]; r.uy = (float) S.uy[k];
 		r.id = S.id[k];
@@ -692,7 +707,7 @@ struct Mix {
 	static __device__ __forceinline__ void to_spill_vals(const Rec &r, const Grid &g,
 			double &x, double &y, double &ux, double &uy)
 	{
-		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
+		int cx = r.cell & ((1 << g.lcx) - 1), cy = r.cell >> g.lcx;
 		x = ((double) cx + (double) r.ox) * g.dx;
 		y = ((double) cy + (double) r.oy) * g.dy;
 		ux = r.ux; uy = r.uy;
@@ -703,7 +718,7 @@ struct Mix {
 	static __device__ __forceinline__ void to_spill_rec(const Rec &r, const Grid &g,
 			double &x, double &y, double &ux, double &uy)
 	{
-		int cx = r.cell & (g.nx - 1), cy = r.cell >> g.lnx;
+		int cx = r.cell & ((1 << g.lcx) - 1), cy = r.cell >> g.lcx;
 		x = (double) cx + (double) r.ox;
 		y = (double) cy + (double) r.oy;
 		ux = r.ux; uy = r.uy;
@@ -711,8 +726,8 @@ struct Mix {
 
 	static __device__ __forceinline__ int cell_of(const Rec &r, const Grid &g, int &cx, int &cy)
 	{
-		cx = r.cell & (g.nx - 1);
-		cy = r.cell >> g.lnx;
+		cx = r.cell & ((1 << g.lcx) - 1);
+		cy = r.cell >> g.lcx;
 		return 0;
 	}
 };
@@ -721,7 +736,8 @@ struct Mix {
 
 // Ids: whether the species' store keeps particle ids (always for F64).
 // P: particles per thread per chunk (a chunk is kPushThreads * P particles).
-template <class F, int MinBlocks = F::kMinBlocks, bool Ids = true, int P = kPPT>
+// GP2: nx and ny are powers of two (the mixed form wraps cells with a mask).
+template <class F, int MinBlocks = F::kMinBlocks, bool Ids = true, int P = kPPT, bool GP2 = true>
 __global__ void __launch_bounds__(kPushThreads, MinBlocks)
 k_push(const PushArgs a)
 {
@@ -752,8 +768,10 @@ k_push(const PushArgs a)
 	}
 	const int H = g.halo;
 	const int W = g.tx + 2 * H + 1;
-	const int tx0 = (t & (g.ntx - 1)) << g.ltx;
-	const int ty0 = (t >> (g.lnx - g.ltx)) << g.lty;
+	int ttx, tty;
+	tile_rc(g, t, ttx, tty);
+	const int tx0 = ttx << g.ltx;
+	const int ty0 = tty << g.lty;
 	const bool ids = Ids;
 	const size_t sb = F::stage_bytes(ids, kChunk);
 	// bulk-copy destinations need 16-byte alignment; the host adds 128
@@ -769,14 +787,12 @@ k_push(const PushArgs a)
 	const int n = T.cnt[t];
 	const int64_t base = T.base[t];
 	const int nchunks = (n + kChunk - 1) / kChunk;
-	const int ltx_n = g.lnx - g.ltx;                 // log2 tiles per row
-	const int ttx = t & (g.ntx - 1), tty = t >> ltx_n;
 	// neighbours are distinct tiles only with at least 3 tiles per side
 	const bool nb_ok = g.ntx >= 3 && g.nty >= 3;
 	if(threadIdx.x < 9 && nb_ok)
 	{
 		int dx = (int) threadIdx.x % 3 - 1, dy = (int) threadIdx.x / 3 - 1;
-		int nt = (((tty + dy) & (g.nty - 1)) << ltx_n) + ((ttx + dx) & (g.ntx - 1));
+		int nt = wrapn(tty + dy, g.nty) * g.ntx + wrapn(ttx + dx, g.ntx);
 		s_nbase[threadIdx.x] = T.base[nt];
 		s_ncap[threadIdx.x] = T.cap[nt];
 	}
@@ -852,7 +868,7 @@ k_push(const PushArgs a)
 			dest[k] = -1;
 			if(valid)
 			{
-				typename F::Out o = F::push(a, s, rec[k], tx0, ty0, Etile);
+				typename F::Out o = F::template push<GP2>(a, s, rec[k], tx0, ty0, Etile);
 				err |= o.err;
 				F::deposit(a, s, fsm, W, H, tx0, ty0, o);
 				dest[k] = o.dest;
@@ -884,12 +900,17 @@ k_push(const PushArgs a)
 				at = base + wb + __popc(bs[k] & lanemask_lt());
 			else if(move)
 			{
+				// the neighbour table covers the 3 x 3 tiles around this
+				// one; a move across the grid's edge reads the tile's own
+				// entries instead (the same values)
 				const int d = dest[k];
-				const int ddx = ((d & (g.ntx - 1)) - ttx + 1) & (g.ntx - 1);
-				const int ddy = ((d >> ltx_n) - tty + 1) & (g.nty - 1);
+				int dtx, dty;
+				tile_rc(g, d, dtx, dty);
+				const int ddx = dtx - ttx + 1;
+				const int ddy = dty - tty + 1;
 				int64_t db;
 				int32_t dc;
-				if(nb_ok && ddx < 3 && ddy < 3)
+				if(nb_ok && (unsigned) ddx < 3u && (unsigned) ddy < 3u)
 				{
 					db = s_nbase[ddy * 3 + ddx];
 					dc = s_ncap[ddy * 3 + ddx];
@@ -961,7 +982,7 @@ k_spill(const SpillArgs sa)
 			if(valid)
 			{
 				r = F::from_spill(S, k, g);
-				o = F::push(a, s, r, 0, 0, nullptr);
+				o = F::template push<false>(a, s, r, 0, 0, nullptr);
 				if(o.err) set_status(a.status, o.err);
 				F::deposit(a, s, nullptr, 0, 0, 0, 0, o);
 			}

@@ -54,7 +54,7 @@ enum cpic_status {
  * library, 2 particles per thread.  No reference counterpart for the last
  * four (the reference's blocks are MPI ranks and plasma chunks). */
 typedef struct cpic_params {
-	int64_t nx, ny;          /* grid.points */
+	int64_t nx, ny;          /* grid.points: any size, 4 ... 16384 */
 	double Lx, Ly;           /* simulation.space_length */
 	double dt;               /* simulation.time_step */
 	double e0;               /* constants.vacuum_permittivity */
@@ -62,7 +62,8 @@ typedef struct cpic_params {
 	int64_t plasma_chunks;   /* simulation.plasma_chunks (sets umax) */
 	int64_t cycles;          /* simulation.cycles */
 	int32_t precision;       /* enum cpic_precision */
-	int32_t tile_x, tile_y;  /* cells per tile, powers of two; 0 = auto */
+	int32_t tile_x, tile_y;  /* cells per tile, equal powers of two dividing
+	                          * nx and ny; 0 = auto */
 	int32_t halo;            /* deposit halo in cells; 0 = auto */
 	int32_t track_ids;       /* keep a particle id per particle (MIXED) */
 	int32_t particles_per_thread; /* fused kernel instance: 1, 2 or 4; 0 = 2 */

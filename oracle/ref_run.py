@@ -53,7 +53,7 @@ simulation = {
 }
 constants = { light_speed = 1.0; vacuum_permittivity = 1.0 }
 """ % (",\n".join(sp), float(case["B"][0]), float(case["B"][1]), float(case["B"][2]), case["nx"],
-       case["ny"], cycles, float(case["dt"]), L, L)
+       case["ny"], cycles, float(case["dt"]), L, float(case.get("Ly", L)))
     with open(path, "w") as f:
         f.write(txt)
 

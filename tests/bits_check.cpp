@@ -108,6 +108,31 @@ int main()
 	}
 	check_split(0.0, 30);
 	check_split(-0.0, 30);
+	// tile-row division: every n up to 4096 against t / n, for t over the
+	// first rows, the last rows of a 4096-row grid and random indices
+	for(uint32_t n = 1; n <= 4096; n++)
+	{
+		uint32_t mul;
+		int sh;
+		div_init(n, mul, sh);
+		auto one = [&](uint32_t t) {
+			checked++;
+			handled++;
+			if(div_q(t, mul, sh) != t / n)
+			{
+				if(bad < 10)
+					std::printf("div %u / %u\n", t, n);
+				bad++;
+			}
+		};
+		for(uint32_t t = 0; t < 3 * n + 7; t++)
+			one(t);
+		for(uint32_t t = 4093 * n; t < 4096 * n; t++)
+			one(t);
+		for(int k = 0; k < 200; k++)
+			one((uint32_t) (rng() % (1u << 30)));
+		one((1u << 30) - 1);
+	}
 	std::printf("%ld mismatches of %ld handled (%ld checked)\n", bad, handled, checked);
 	return bad != 0;
 }

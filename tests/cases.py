@@ -13,11 +13,14 @@ TWO_PI = 2.0 * math.pi
 
 
 def two_stream(nx=64, ny=64, n=10240, v0=0.2, vth=0.0, amp=0.01, dt=0.05, L=TWO_PI, seed=1234,
-               steps=200):
-    """Two-stream instability (64x64, 10240 electrons: the CPU-runnable case)."""
-    q = -L * L / n
-    x, y, ux, uy = _lib.init_two_stream(seed, 0, n, L, L, v0, vth, amp)
-    return dict(nx=nx, ny=ny, L=L, dt=dt, B=(0.0, 0.0, 0.0), steps=steps,
+               steps=200, Ly=None):
+    """Two-stream instability (64x64, 10240 electrons: the CPU-runnable case).
+    Ly: the domain's y length (default L; give L * ny / nx for square cells
+    on a rectangular grid, as the reference's Y weights use dx)."""
+    Ly = L if Ly is None else Ly
+    q = -L * Ly / n
+    x, y, ux, uy = _lib.init_two_stream(seed, 0, n, L, Ly, v0, vth, amp)
+    return dict(nx=nx, ny=ny, L=L, Ly=Ly, dt=dt, B=(0.0, 0.0, 0.0), steps=steps,
                 species=[dict(q=q, m=-q, x=x, y=y, ux=ux, uy=uy)])
 
 
@@ -34,10 +37,15 @@ def two_species(nx=512, ny=512, ppc=16, vth_e=0.05, mass_ratio=100.0, vth_i=0.00
                          dict(q=-qe, m=mass_ratio * me, x=xi, y=yi, ux=uxi, uy=uyi)])
 
 
+def lengths(case):
+    """(Lx, Ly) of a case."""
+    return case["L"], case.get("Ly", case["L"])
+
+
 def make_gpu(case, precision=_lib.FP64, **kw):
-    L = case["L"]
-    ctx = _lib.Context(case["nx"], case["ny"], L, L, case["dt"], 1.0, case["B"], precision=precision,
-                       **kw)
+    Lx, Ly = lengths(case)
+    ctx = _lib.Context(case["nx"], case["ny"], Lx, Ly, case["dt"], 1.0, case["B"],
+                       precision=precision, **kw)
     for s in case["species"]:
         ctx.add_species(s["q"], s["m"], s["x"], s["y"], s["ux"], s["uy"])
     return ctx
@@ -45,8 +53,8 @@ def make_gpu(case, precision=_lib.FP64, **kw):
 
 def make_oracle(case, lossy=False):
     from oracle.oracle import Oracle
-    L = case["L"]
-    o = Oracle(case["nx"], case["ny"], L, L, case["dt"], 1.0, case["B"], lossy=lossy)
+    Lx, Ly = lengths(case)
+    o = Oracle(case["nx"], case["ny"], Lx, Ly, case["dt"], 1.0, case["B"], lossy=lossy)
     for s in case["species"]:
         o.add_species(s["q"], s["m"], s["x"], s["y"], s["ux"], s["uy"])
     return o

@@ -103,11 +103,13 @@ def test_no_device_reports_enodev(lib):
 
 def test_invalid_params_rejected(lib):
     p = _lib.Params()
-    p.nx, p.ny = 48, 64                 # not a power of two
+    p.nx, p.ny = 3, 64                  # below the 4-cell minimum
     p.Lx = p.Ly = 1.0
     p.dt = 0.1
     p.e0 = 1.0
     h = ctypes.c_void_p()
+    assert lib.cpic_create(ctypes.byref(p), ctypes.byref(h)) == -1
+    p.nx = 1 << 15                      # above 16384
     assert lib.cpic_create(ctypes.byref(p), ctypes.byref(h)) == -1
     p.nx = 64
     p.B[0] = 1.0                        # in-plane B: the reference rejects u_z != 0

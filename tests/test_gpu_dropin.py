@@ -106,8 +106,20 @@ def test_harmonic_driver_trace(out):
     assert worst <= 1e-6, worst          # %+e prints 7 significant digits
 
 
-def conf_with(path, cycles, host_sync, output_dir=None, stop_sem=0.0):
+def conf_with(path, cycles, host_sync, output_dir=None, stop_sem=0.0, grid=None):
+    """The two-stream .conf with the given cycles and options; grid = (nx,
+    ny, particles) sets the grid (square cells: Ly = 2 pi ny / nx) and the
+    electron count and charge to match."""
     txt = open(TWO_STREAM_CONF).read()
+    if grid:
+        nx, ny, n = grid
+        Lx, Ly = cases.TWO_PI, cases.TWO_PI * ny / nx
+        q = Lx * Ly / n
+        txt = re.sub(r"points = \[\d+, \d+\]", "points = [%d, %d]" % (nx, ny), txt)
+        txt = re.sub(r"particles = \d+", "particles = %d" % n, txt)
+        txt = re.sub(r"charge = [-0-9.e]+", "charge = %r" % -q, txt)
+        txt = re.sub(r"mass = [-0-9.e]+", "mass = %r" % q, txt)
+        txt = re.sub(r"space_length = \[[^]]*\]", "space_length = [%r, %r]" % (Lx, Ly), txt)
     txt = re.sub(r"cycles = \d+", "cycles = %d" % cycles, txt)
     txt = re.sub(r"host_sync = \d+", "host_sync = %d" % host_sync, txt)
     txt = re.sub(r"stop_SEM = [0-9.]+", "stop_SEM = %r" % stop_sem, txt)
@@ -211,6 +223,37 @@ def test_cpic_main_writes_fields_matching_oracle(out):
             assert abs(we - owe) <= 1e-10 * owe, it
             # the next output is after the next step's field solve (the
             # oracle's next step solves the same rho again: no change)
+            o.step()
+            o.stage_field_E()
+
+
+def test_cpic_main_grid_not_power_of_two(out):
+    """cpic's own main on a 48 x 40 grid (the reference's solver takes any
+    size): every written field against the oracle, rho, phi and E within
+    1e-12 of their max norm at the first output and the field energy within
+    1e-10 at every one."""
+    steps, nx, ny, n = 12, 48, 40, 48 * 40 * 4
+    with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "tests", "_dropin")) as d:
+        od = os.path.join(d, "out")
+        conf = os.path.join(d, "grid.conf")
+        conf_with(conf, steps, 0, output_dir=od, grid=(nx, ny, n))
+        r = run(out, "cpic_gpu", [conf])
+        assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+        case = cases.two_stream(nx=nx, ny=ny, n=n, seed=1, Ly=cases.TWO_PI * ny / nx)
+        o = cases.make_oracle(case)
+        o.pre_step()
+        cell = (cases.TWO_PI / nx) ** 2
+        for it in range(steps):
+            rho, phi = read_field(od, it, "rho"), read_field(od, it, "phi")
+            ex, ey = read_field(od, it, "E_X"), read_field(od, it, "E_Y")
+            assert rho.shape == (ny, nx) and ex.shape == (ny, nx)
+            oex, oey = o.E()
+            if it == 0:
+                for a, b in ((rho, o.rho()), (phi, o.phi()), (ex, oex[:ny]), (ey, oey[:ny])):
+                    assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+            we = 0.5 * np.sum(ex ** 2 + ey ** 2) * cell
+            owe = 0.5 * np.sum(oex[:ny] ** 2 + oey[:ny] ** 2) * cell
+            assert abs(we - owe) <= 1e-10 * owe, it
             o.step()
             o.stage_field_E()
 

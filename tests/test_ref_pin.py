@@ -10,7 +10,8 @@ E, positions and velocities after the iteration-0 half kick; full steps
 from the reference's own state and fields; rho deposited in the
 reference's particle order (conflict-free variant, and the shipped lossy
 variant against the oracle's lossy mode); field energy over 200 steps
-within 1e-10; and the reference's committed harmonic-oscillator traces
+within 1e-10; grids whose sides are not powers of two; and the
+reference's committed harmonic-oscillator traces
 (test/harmonic/harm.r0x, harm.E0x) to their printed precision.
 """
 import os
@@ -28,8 +29,8 @@ pytestmark = pytest.mark.skipif(not os.path.isdir(REF) or not refrun.available()
 def oracle_from(case, species_states, lossy=False):
     """Oracle with the given per-species arrays (already in the order wanted)."""
     from oracle.oracle import Oracle
-    L = case["L"]
-    o = Oracle(case["nx"], case["ny"], L, L, case["dt"], 1.0, case["B"], lossy=lossy)
+    Lx, Ly = cases.lengths(case)
+    o = Oracle(case["nx"], case["ny"], Lx, Ly, case["dt"], 1.0, case["B"], lossy=lossy)
     for s, st in zip(case["species"], species_states):
         o.add_species(s["q"], s["m"], st["x"], st["y"], st["ux"], st["uy"])
     return o
@@ -115,6 +116,35 @@ def test_two_species_bz_energy():
     for _ in range(100):
         o.step()
         we.append(o.diag()["WE"])
+    rel = np.max(np.abs(np.array(we) - ref["energy"]) / ref["energy"])
+    assert rel <= 1e-10, rel
+
+
+@pytest.mark.parametrize("nx,ny", [(48, 40), (25, 15)])
+def test_grid_not_power_of_two(nx, ny):
+    """Grids whose sides are not powers of two (the reference's FFTW solver
+    takes any size): pre-step fields bit-exact, the particles after two
+    steps bit-exact, field energy over 60 steps within 1e-10.  Square cells
+    (Ly = L ny / nx), as the reference's Y weights use dx."""
+    L = cases.TWO_PI
+    case = cases.two_stream(nx=nx, ny=ny, n=nx * ny * 4, Ly=L * ny / nx)
+    ref = refrun.run(case, 60, dumps=(2,))
+    o = cases.make_oracle(case)
+    o.pre_step()
+    pre = ref["pre"]
+    assert np.array_equal(o.rho(), pre["rho"])
+    assert np.array_equal(o.phi(), pre["phi"])
+    ex, ey = o.E()
+    assert np.array_equal(ex, pre["Ex"]) and np.array_equal(ey, pre["Ey"])
+    we = []
+    for k in range(60):
+        o.step()
+        we.append(o.diag()["WE"])
+        if k == 1:
+            r = refrun.by_id(ref[2]["species"][0])
+            x, y, ux, uy = o.particles(0)
+            for a, b in ((x, r["x"]), (y, r["y"]), (ux, r["ux"]), (uy, r["uy"])):
+                assert np.array_equal(a, b)
     rel = np.max(np.abs(np.array(we) - ref["energy"]) / ref["energy"])
     assert rel <= 1e-10, rel
 
