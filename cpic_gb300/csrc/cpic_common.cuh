@@ -2,11 +2,14 @@
 // FP64 and mixed-precision kernel translation units and the host context.
 //
 // Particle store: per species, structure of arrays partitioned into tiles of
-// TX x TY cells.  Tile t owns slots [base[t], base[t] + cap[t]) of every
-// array; the first cnt[t] slots hold the particles whose cell lies in the
-// tile.  One step moves particles that leave their tile by appending them
-// to the destination tile (slot reserved with an atomic on app[D]) and
-// compacting the stayers in place; a fix-up pass closes the gap.  Particles
+// TX x TY cells.  Tile t owns a main region, slots [base[t], base[t] +
+// cap[t]) of every array, whose first cnt[t] slots hold particles whose cell
+// lies in the tile, and an arrivals region in each of two buffers after the
+// main regions.  One step reads a tile's main region and the arrivals the
+// previous step left in one buffer, compacts the stayers in place at the
+// front of the main region, and appends the particles that leave to their
+// destination tile's arrivals in the other buffer (slot reserved with an
+// atomic on its count): no pass between steps has to close gaps.  Particles
 // that find no room go to a spill list that a generic kernel keeps pushing
 // until the host rebuilds the layout with a full counting sort.
 //
@@ -71,12 +74,20 @@ struct StoreMix {
 	int32_t *id;     // optional (nullptr when ids are not tracked)
 };
 
+// Each tile owns a main region of the store, which its own block compacts in
+// place, and two arrivals regions (buffers 0 and 1, abuf1 slots apart) into
+// which other blocks append the particles that move in.  A step's fused
+// kernel reads the main region and the arrivals that the previous step left
+// in buffer r, and appends this step's movers to buffer 1 - r, so no pass
+// between steps has to close the gaps the movers leave.
 struct Tiles {
-	int64_t *base;   // first slot of the tile
-	int32_t *cap;    // slots owned by the tile
-	int32_t *cnt;    // particles at the start of the step
-	int32_t *app;    // append cursor (starts at cnt)
-	int32_t *stay;   // stayers after the push
+	int64_t *base;   // first slot of the tile's main region
+	int32_t *cap;    // slots of the main region
+	int32_t *cnt;    // particles in the main region at the start of the step
+	int64_t *abase;  // first slot of the tile's arrivals region in buffer 0
+	int32_t *acap;   // slots of each arrivals region
+	int32_t *acnt[2];   // particles in the arrivals region of buffer 0 and 1
+	int64_t abuf1;   // slot offset of buffer 1 from buffer 0
 	int32_t *order;  // tile taken by block b of the fused kernel (a permutation)
 };
 
@@ -125,6 +136,7 @@ struct SpeciesStep {
 struct PushArgs {
 	Grid g;
 	int nspecies;
+	int arr_r;           // arrivals buffer read by this step (movers go to 1 - arr_r)
 	int iter;            // 0 -> backward half step, no move
 	double dt;
 	float cdx_f, cdy_f;  // dt/dx, dt/dy (mixed form)

@@ -1,6 +1,7 @@
 // cpic_ctx.cu -- host context and C ABI (include/cpic_gpu.h), plus the
-// generic device kernels: tile fix-up, counting-sort rebuild of the
-// particle store, host views and FP64 diagnostics.
+// generic device kernels: the merge of pending arrivals into the main
+// regions, counting-sort rebuild of the particle store, host views and FP64
+// diagnostics.
 //
 // Compiled with --fmad=false: the tile of an FP64 particle computed here
 // must agree bit for bit with the one the push kernel computes.
@@ -61,15 +62,12 @@ struct cpic_ctx {
 	double qlo_mul, qinv_lo;  // FP64 form: remainder-word scales
 	bool wq_exact;            // mixed form: integer charge multiples
 	cudaStream_t stream;
-	// the tile fix-up of a step may run on `side`, overlapping the next
-	// step's field solve (which touches no particle); `stream` waits for
-	// ev_fix (join_fixup) before anything reads the particles again
-	cudaStream_t side;
-	cudaEvent_t ev_push, ev_fix;
-	bool fix_pending;
 	int order_mode;           // tile order: 0 undecided, 1 computed each step, 2 kept
 	int nspecies;
 	SpeciesHost sp[kMaxSpecies];
+	// parity of the double-buffered spill lists and arrivals buffers: the
+	// next particle stage reads spill[spill_cur] and arrivals buffer
+	// spill_cur, and writes the other ones
 	int spill_cur;
 	// fields
 	long long *rho;           // ny x nx fixed point
@@ -94,27 +92,37 @@ struct cpic_ctx {
 
 // ------------------------------------------------------------- kernels
 
-// Closes the gap between the compacted stayers and the appended movers.
+// Moves the arrivals in buffer a.arr_r into each tile's main region, so that
+// every pass over the main regions sees all the species' particles (before a
+// host read, a rebuild or a re-layout); arrivals the main region has no room
+// for go to the spill list a.spill_out (cell units for the mixed form).
 template <class F>
-__global__ void k_fixup(const PushArgs a)
+__global__ void k_merge(const PushArgs a)
 {
-	int s = blockIdx.y, t = blockIdx.x;
+	const int s = blockIdx.y, t = blockIdx.x;
 	const Tiles &T = a.tiles[s];
-	int cnt_old = T.cnt[t], stay = T.stay[t];
-	int app = min(T.app[t], T.cap[t]);
-	int inc = app - cnt_old;
-	int gap = cnt_old - stay;
-	int k = min(gap, inc);
-	int64_t b = T.base[t];
-	for(int i = threadIdx.x; i < k; i += blockDim.x)
+	const int r = a.arr_r;
+	const int na = min(T.acnt[r][t], T.acap[t]), nm = T.cnt[t];
+	const int k = min(na, max(0, T.cap[t] - nm));
+	const int64_t src = T.abase[t] + (r ? T.abuf1 : 0), dst = T.base[t] + nm;
+	for(int i = threadIdx.x; i < na; i += blockDim.x)
 	{
-		typename F::Rec r = F::load(a, s, b + app - k + i);
-		F::store(a, s, b + stay + i, r);
+		typename F::Rec rec = F::load(a, s, src + i);
+		if(i < k)
+			F::store(a, s, dst + i, rec);
+		else
+		{
+			double x, y, ux, uy;
+			F::to_spill_rec(rec, a.g, x, y, ux, uy);
+			if(!spill_push(a.spill_out[s], x, y, ux, uy, rec.id))
+				set_status(a.status, ST_SPILL_FULL);
+		}
 	}
+	__syncthreads();
 	if(threadIdx.x == 0)
 	{
-		T.cnt[t] = stay + inc;
-		T.app[t] = stay + inc;
+		T.cnt[t] = nm + k;
+		T.acnt[r][t] = 0;
 	}
 }
 
@@ -125,9 +133,11 @@ __global__ void k_fixup(const PushArgs a)
 // 1.1x the mean count go first and tiles below 0.9x the mean go last, each
 // group heaviest first in steps of 1/16 of the mean; the rest keep tile
 // order in between, so a uniform plasma keeps the identity order (and
-// neighbouring tiles, which write into each other's free tails, run
-// together).  A stable counting sort, so the order is a function of the
-// counts alone.  Which block takes which tile changes no result.
+// neighbouring tiles, which write into each other's arrivals, run
+// together).  A tile's count is its main region's plus the arrivals in
+// buffer abuf (what the next launch reads).  A stable counting sort, so the
+// order is a function of the counts alone.  Which block takes which tile
+// changes no result.
 constexpr int kOrderKeys = 512;
 constexpr int kOrderMid = kOrderKeys - 1 - 255;      // bucket of the middle class
 constexpr int kOrderThreads = 1024;
@@ -151,7 +161,7 @@ __device__ __forceinline__ int order_bucket(int32_t cnt, int ntiles, long long s
 // parallel; a uniform layout (every tile in the middle class) writes the
 // identity at once; otherwise warp 0 scans the bucket counts and scatters
 // from the buckets kept in shared memory.
-__global__ void __launch_bounds__(kOrderThreads) k_tile_order(const PushArgs a, int ntiles)
+__global__ void __launch_bounds__(kOrderThreads) k_tile_order(const PushArgs a, int ntiles, int abuf)
 {
 	const Tiles &T = a.tiles[blockIdx.x];
 	__shared__ uint16_t s_b[kOrderMaxTiles];
@@ -164,7 +174,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_tile_order(const PushArgs a, 
 	for(int k = 0; k < kOrderPer; k++)
 	{
 		const int i = k * kOrderThreads + tid;
-		c[k] = i < ntiles ? T.cnt[i] : 0;
+		c[k] = i < ntiles ? T.cnt[i] + T.acnt[abuf][i] : 0;
 		sum += c[k];
 	}
 	for(int o = 16; o > 0; o >>= 1)
@@ -765,6 +775,7 @@ static PushArgs make_args(cpic_ctx *c, int cur_spill)
 	memset(&a, 0, sizeof(a));
 	a.g = c->g;
 	a.nspecies = c->nspecies;
+	a.arr_r = c->spill_cur;
 	for(int s = 0; s < c->nspecies; s++)
 	{
 		a.tiles[s] = c->sp[s].tiles;
@@ -1013,28 +1024,42 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	// capacities: slack_pct % slack (25 % at first, doubled after every
 	// rebuild forced by an overflow, up to 200 %) plus 64 slots, rounded
 	// to 32
-	std::vector<int64_t> hb(nt);
-	std::vector<int32_t> hcap(nt);
-	int64_t total = 0, n = 0;
+	// arrivals regions: two buffers after the main regions, each tile
+	// with room for a quarter of its count (a step moves about a tenth of
+	// the particles of the two-stream workload between tiles), more as
+	// overflows raise the slack (a quarter of it in each buffer, so that a
+	// store at 200 % slack holds 4x its particles: two such stores, the
+	// current one and the alternate, of both forms fit in HBM at 2048^2)
+	std::vector<int64_t> hb(nt), hab(nt);
+	std::vector<int32_t> hcap(nt), hacap(nt);
+	int64_t total = 0, atotal = 0, n = 0;
+	const int arr_pct = std::max(25, c->slack_pct / 4);
 	for(int t = 0; t < nt; t++)
 	{
 		int64_t cap = hc[t] + hc[t] * c->slack_pct / 100 + 64;
 		cap = (cap + 31) & ~(int64_t) 31;
-		if(cap > INT32_MAX) return CPIC_ECAPACITY;
+		int64_t acap = hc[t] * arr_pct / 100 + 64;
+		acap = (acap + 31) & ~(int64_t) 31;
+		if(cap > INT32_MAX || acap > INT32_MAX) return CPIC_ECAPACITY;
 		hb[t] = total;
 		hcap[t] = (int32_t) cap;
+		hab[t] = atotal;
+		hacap[t] = (int32_t) acap;
 		total += cap;
+		atotal += acap;
 		n += hc[t];
 	}
+	for(int t = 0; t < nt; t++) hab[t] += total;
+	const int64_t slots = total + 2 * atotal;
 
 	// the alternate store receives the new layout
 	bool have_alt = mix ? S.mix_alt.ux != nullptr : S.f64_alt.ux != nullptr;
-	if(S.cap_alt < total || !have_alt)
+	if(S.cap_alt < slots || !have_alt)
 	{
 		free_store(c, S, true);
-		int r = alloc_store(c, S, total, true);
+		int r = alloc_store(c, S, slots, true);
 		if(r) return r;
-		S.cap_alt = total;
+		S.cap_alt = slots;
 	}
 	int64_t *nbase;
 	int32_t *ncap;
@@ -1129,9 +1154,13 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	CK(cudaGetLastError());
 	CK(cudaMemsetAsync(spin.count, 0, sizeof(int32_t), st));
 	CK(cudaMemcpyAsync(S.tiles.cnt, newcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
-	CK(cudaMemcpyAsync(S.tiles.app, newcnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
 	CK(cudaMemcpyAsync(S.tiles.base, nbase, nt * sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
 	CK(cudaMemcpyAsync(S.tiles.cap, ncap, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+	CK(cudaMemcpyAsync(S.tiles.abase, hab.data(), nt * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(S.tiles.acap, hacap.data(), nt * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(S.tiles.acnt[0], 0, nt * sizeof(int32_t), st));
+	CK(cudaMemsetAsync(S.tiles.acnt[1], 0, nt * sizeof(int32_t), st));
+	S.tiles.abuf1 = atotal;
 	CK(cudaStreamSynchronize(st));
 	cudaFree(nbase); cudaFree(ncap); cudaFree(newcnt); cudaFree(fill);
 	// swap stores; the old one becomes the alternate
@@ -1142,22 +1171,53 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	return CPIC_OK;
 }
 
+// Every species' pending arrivals (buffer spill_cur) into the main regions,
+// overflow to spill[spill_cur] (the list the next stage and a rebuild read).
+static int merge_arrivals(cpic_ctx *c)
+{
+	if(c->nspecies == 0) return CPIC_OK;
+	PushArgs a = make_args(c, c->spill_cur);
+	for(int s = 0; s < c->nspecies; s++)
+		a.spill_out[s] = c->sp[s].spill[c->spill_cur];
+	dim3 grid(c->ntiles, c->nspecies);
+	if(c->precision == CPIC_MIXED)
+		k_merge<Mix><<<grid, 256, 0, c->stream>>>(a);
+	else
+		k_merge<F64><<<grid, 256, 0, c->stream>>>(a);
+	CK(cudaGetLastError());
+	return CPIC_OK;
+}
+
+// After the context's stream has been synchronised: rebuilds the layout of
+// every species whose spill list holds records (merging the pending arrivals
+// first, since a rebuild reads the main regions and the spill list).
 static int rebuild_if_spilled(cpic_ctx *c)
 {
 	c->last_spill = 0;
+	bool any = false;
 	for(int s = 0; s < c->nspecies; s++)
 	{
 		int32_t ns = 0;
 		CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
 				cudaMemcpyDeviceToHost));
 		c->last_spill += ns;
+		any = any || ns > 0;
+	}
+	if(!any) return CPIC_OK;
+	int r = merge_arrivals(c);
+	if(r) return r;
+	CK(cudaStreamSynchronize(c->stream));
+	for(int s = 0; s < c->nspecies; s++)
+	{
+		int32_t ns = 0;
+		CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
+				cudaMemcpyDeviceToHost));
 		if(ns > 0)
 		{
 			// a tile overflowed: more headroom from now on
 			c->rebuilds++;
 			c->slack_pct = std::min(200, 2 * c->slack_pct);
-			int r = rebuild_species(c, s, false, nullptr, 0);
-			if(r) return r;
+			if((r = rebuild_species(c, s, false, nullptr, 0))) return r;
 		}
 	}
 	return CPIC_OK;
@@ -1183,7 +1243,7 @@ static bool tile_order_pays(const cpic_ctx *c, size_t smem)
 // One fused particle stage (gather, push, re-bin, deposit) without
 // host synchronisation.  deposit_only: the initial charge deposit.
 static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = nullptr,
-		cudaEvent_t ev1 = nullptr, bool overlap = false)
+		cudaEvent_t ev1 = nullptr)
 {
 	cudaStream_t st = c->stream;
 	int64_t ng = (int64_t) c->g.nx * c->g.ny;
@@ -1226,42 +1286,26 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 		CK(launch_push_f64(sa.p, c->ntiles, smem, c->ppt, st));
 	if(ev1) CK(cudaEventRecord(ev1, st));
 	CK(cudaGetLastError());
-	// the tile fix-up: bandwidth-bound, so with `overlap` it runs on the
-	// side stream beside the next step's latency-bound field solve
-	cudaStream_t fs = st;
-	if(overlap)
-	{
-		CK(cudaEventRecord(c->ev_push, st));
-		CK(cudaStreamWaitEvent(c->side, c->ev_push, 0));
-		fs = c->side;
-	}
-	dim3 fg(c->ntiles, c->nspecies);
-	if(c->precision == CPIC_MIXED)
-		k_fixup<Mix><<<fg, 256, 0, fs>>>(sa.p);
-	else
-		k_fixup<F64><<<fg, 256, 0, fs>>>(sa.p);
-	// the next launch's tile order, from the counts the fix-up leaves
+	// the next launch's tile order, from the main regions' counts and the
+	// arrivals this launch left for it
 	if(c->order_mode == 0)
 		c->order_mode = tile_order_pays(c, smem) ? 1 : 2;
 	if(c->order_mode == 1)
-		k_tile_order<<<c->nspecies, kOrderThreads, 0, fs>>>(sa.p, c->ntiles);
+		k_tile_order<<<c->nspecies, kOrderThreads, 0, st>>>(sa.p, c->ntiles, cur ^ 1);
 	CK(cudaGetLastError());
-	if(overlap)
-	{
-		CK(cudaEventRecord(c->ev_fix, c->side));
-		c->fix_pending = true;
-	}
 	c->spill_cur ^= 1;
 	return CPIC_OK;
 }
 
-// The main stream waits for a fix-up left running on the side stream.
-static int join_fixup(cpic_ctx *c)
+// The state host reads and re-layouts walk: every particle in a main region
+// (arrivals merged, the spill list rebuilt into the tiles if anything
+// overflowed).
+static int normalize(cpic_ctx *c)
 {
-	if(!c->fix_pending) return CPIC_OK;
-	c->fix_pending = false;
-	CK(cudaStreamWaitEvent(c->stream, c->ev_fix, 0));
-	return CPIC_OK;
+	int r = merge_arrivals(c);
+	if(r) return r;
+	CK(cudaStreamSynchronize(c->stream));
+	return rebuild_if_spilled(c);
 }
 
 static int field_stage_async(cpic_ctx *c)
@@ -1375,22 +1419,11 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 	bits::div_init((uint32_t) g.ntx, g.ntx_mul, g.ntx_sh);
 	g.pow2 = pow2(g.nx) && pow2(g.ny);
 	c->ntiles = g.ntx * g.nty;
-	// the main stream at the highest priority: the field solve's blocks go
-	// ahead of the fix-up blocks still waiting on the low-priority side
-	int prio_lo = 0, prio_hi = 0;
-	cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-	if(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess
-			|| cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess
-			|| cudaEventCreateWithFlags(&c->ev_push, cudaEventDisableTiming) != cudaSuccess
-			|| cudaEventCreateWithFlags(&c->ev_fix, cudaEventDisableTiming) != cudaSuccess)
+	if(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
 	{
-		if(c->stream) cudaStreamDestroy(c->stream);
-		if(c->side) cudaStreamDestroy(c->side);
-		if(c->ev_push) cudaEventDestroy(c->ev_push);
 		delete c;
 		return CPIC_ECUDA;
 	}
-	c->fix_pending = false;
 	int64_t ng = (int64_t) g.nx * g.ny;
 	int64_t nh = g.nx / 2 + 1;
 	int r = CPIC_OK;
@@ -1486,7 +1519,6 @@ fail:
 CPIC_API void cpic_destroy(cpic_ctx_t *c)
 {
 	if(!c) return;
-	cudaStreamSynchronize(c->side);
 	cudaStreamSynchronize(c->stream);
 	for(int s = 0; s < c->nspecies; s++)
 	{
@@ -1494,7 +1526,8 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 		free_store(c, S, false);
 		free_store(c, S, true);
 		cudaFree(S.tiles.base); cudaFree(S.tiles.cap); cudaFree(S.tiles.cnt);
-		cudaFree(S.tiles.app); cudaFree(S.tiles.stay); cudaFree(S.tiles.order);
+		cudaFree(S.tiles.abase); cudaFree(S.tiles.acap);
+		cudaFree(S.tiles.acnt[0]); cudaFree(S.tiles.acnt[1]); cudaFree(S.tiles.order);
 		free_spill(S.spill[0]);
 		free_spill(S.spill[1]);
 	}
@@ -1504,9 +1537,6 @@ CPIC_API void cpic_destroy(cpic_ctx_t *c)
 	cudaFree(c->cosx); cudaFree(c->cosy); cudaFree(c->green64); cudaFree(c->green32); cudaFree(c->mean);
 	cudaFree(c->status); cudaFree(c->scratch); cudaFree(c->counter); cudaFree(c->counter_pair);
 	if(c->stream) cudaStreamDestroy(c->stream);
-	if(c->side) cudaStreamDestroy(c->side);
-	if(c->ev_push) cudaEventDestroy(c->ev_push);
-	if(c->ev_fix) cudaEventDestroy(c->ev_fix);
 	delete c;
 }
 
@@ -1611,14 +1641,16 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	CK(cudaMalloc(&S.tiles.base, nt * sizeof(int64_t)));
 	CK(cudaMalloc(&S.tiles.cap, nt * sizeof(int32_t)));
 	CK(cudaMalloc(&S.tiles.cnt, nt * sizeof(int32_t)));
-	CK(cudaMalloc(&S.tiles.app, nt * sizeof(int32_t)));
-	CK(cudaMalloc(&S.tiles.stay, nt * sizeof(int32_t)));
+	CK(cudaMalloc(&S.tiles.abase, nt * sizeof(int64_t)));
+	CK(cudaMalloc(&S.tiles.acap, nt * sizeof(int32_t)));
+	CK(cudaMalloc(&S.tiles.acnt[0], nt * sizeof(int32_t)));
+	CK(cudaMalloc(&S.tiles.acnt[1], nt * sizeof(int32_t)));
 	CK(cudaMalloc(&S.tiles.order, nt * sizeof(int32_t)));
 	k_iota<<<grid_blocks(nt), 256, 0, st>>>(nt, S.tiles.order);
 	CK(cudaGetLastError());
 	CK(cudaMemsetAsync(S.tiles.cnt, 0, nt * sizeof(int32_t), st));
-	CK(cudaMemsetAsync(S.tiles.app, 0, nt * sizeof(int32_t), st));
-	CK(cudaMemsetAsync(S.tiles.stay, 0, nt * sizeof(int32_t), st));
+	CK(cudaMemsetAsync(S.tiles.acnt[0], 0, nt * sizeof(int32_t), st));
+	CK(cudaMemsetAsync(S.tiles.acnt[1], 0, nt * sizeof(int32_t), st));
 	// room for an eighth of the species to overflow between two host checks
 	int32_t scap = (int32_t) std::max<int64_t>(65536, n / 8);
 	const int cu = c->precision == CPIC_MIXED ? 1 : 0;
@@ -1706,16 +1738,12 @@ static int run_steps(cpic_ctx *c, int64_t nsteps)
 	for(int64_t k = 0; k < nsteps; k++)
 	{
 		if(c->p.cycles > 0 && c->iter >= c->p.cycles) return CPIC_EDONE;
-		// this step's field solve overlaps the previous step's tile
-		// fix-up; the join orders it before this step's particle stage
 		int r = field_stage_async(c);
 		if(r) return r;
-		if((r = join_fixup(c))) return r;
-		if((r = plasma_stage_async(c, false, nullptr, nullptr, true))) return r;
+		if((r = plasma_stage_async(c, false))) return r;
 		c->iter++;
 		if((k & 7) == 7 || k + 1 == nsteps)
 		{
-			if((r = join_fixup(c))) return r;
 			if((r = check_status(c))) return r;
 			if((r = rebuild_if_spilled(c))) return r;
 		}
@@ -1727,9 +1755,7 @@ CPIC_API int cpic_run(cpic_ctx_t *c, int64_t nsteps)
 {
 	if(!c) return CPIC_EINVAL;
 	if(!c->prepared) return CPIC_ESTATE;
-	int r = run_steps(c, nsteps);
-	int rj = join_fixup(c);
-	return r ? r : rj;
+	return run_steps(c, nsteps);
 }
 
 CPIC_API int64_t cpic_iter(const cpic_ctx_t *c) { return c ? c->iter : -1; }
@@ -1744,10 +1770,12 @@ CPIC_API int cpic_get_particles(cpic_ctx_t *c, int s, double *x, double *y, doub
 		double *uy)
 {
 	if(!c || s < 0 || s >= c->nspecies) return CPIC_EINVAL;
+	int r = normalize(c);
+	if(r) return r;
 	int64_t n = c->sp[s].n;
 	int nt = c->ntiles;
 	// scratch: the four FP64 columns, then the per-tile prefix (store order)
-	int r = ensure_scratch(c, 4 * (size_t) std::max<int64_t>(n, 1) + nt);
+	r = ensure_scratch(c, 4 * (size_t) std::max<int64_t>(n, 1) + nt);
 	if(r) return r;
 	cudaStream_t st = c->stream;
 	double *d = c->scratch;
@@ -1812,7 +1840,9 @@ CPIC_API int cpic_gather_E(cpic_ctx_t *c, int s, double *ex, double *ey)
 	if(!c || s < 0 || s >= c->nspecies) return CPIC_EINVAL;
 	if(c->precision == CPIC_MIXED && !c->p.track_ids) return CPIC_EINVAL;
 	int64_t n = c->sp[s].n;
-	int r = ensure_scratch(c, 2 * (size_t) std::max<int64_t>(n, 1));
+	int r = normalize(c);
+	if(r) return r;
+	r = ensure_scratch(c, 2 * (size_t) std::max<int64_t>(n, 1));
 	if(r) return r;
 	cudaStream_t st = c->stream;
 	SpeciesHost &S = c->sp[s];
@@ -1912,7 +1942,9 @@ CPIC_API int cpic_cell_counts(cpic_ctx_t *c, int64_t *counts)
 {
 	if(!c || !counts) return CPIC_EINVAL;
 	int64_t ng = (int64_t) c->g.nx * c->g.ny;
-	int r = ensure_scratch(c, ng);
+	int r = normalize(c);
+	if(r) return r;
+	r = ensure_scratch(c, ng);
 	if(r) return r;
 	cudaStream_t st = c->stream;
 	unsigned long long *d = (unsigned long long *) c->scratch;
@@ -1936,7 +1968,9 @@ CPIC_API int cpic_diag(cpic_ctx_t *c, double *out)
 	if(!c || !out) return CPIC_EINVAL;
 	int nt = c->ntiles, ny = c->g.ny;
 	size_t need = std::max<size_t>(2 * (size_t) ny, 3 * (size_t) nt);
-	int r = ensure_scratch(c, need);
+	int r = normalize(c);
+	if(r) return r;
+	r = ensure_scratch(c, need);
 	if(r) return r;
 	cudaStream_t st = c->stream;
 	std::vector<double> h(need);
@@ -2000,7 +2034,7 @@ CPIC_API int cpic_compact(cpic_ctx_t *c, int32_t slack_pct)
 {
 	if(!c || slack_pct < 0 || slack_pct > 1000) return CPIC_EINVAL;
 	if(!c->prepared) return CPIC_ESTATE;
-	int r = join_fixup(c);
+	int r = normalize(c);
 	if(r) return r;
 	CK(cudaStreamSynchronize(c->stream));
 	c->slack_pct = slack_pct;
@@ -2072,13 +2106,9 @@ CPIC_API int cpic_time_steps(cpic_ctx_t *c, int64_t nsteps, double *ms_total, do
 		CK(cudaEventRecord(f0, st));
 		if((r = field_stage_async(c))) break;
 		CK(cudaEventRecord(f1, st));
-		// the previous step's fix-up ran beside the field solve
-		if((r = join_fixup(c))) break;
-		if((r = plasma_stage_async(c, false, ev[2 + 2 * k], ev[2 + 2 * k + 1], true))) break;
+		if((r = plasma_stage_async(c, false, ev[2 + 2 * k], ev[2 + 2 * k + 1]))) break;
 		c->iter++;
 	}
-	if(r == CPIC_OK) r = join_fixup(c);
-	else join_fixup(c);
 	CK(cudaEventRecord(ev[1], st));
 	CK(cudaEventSynchronize(ev[1]));
 	float tot = 0.0f;

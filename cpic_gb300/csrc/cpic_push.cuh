@@ -15,14 +15,16 @@
 //   Mix : int32 cell + FP32 offset, FP32 velocity; E staged per tile in
 //         shared memory; 32-bit integer weight accumulator.
 //
-// Skeleton per block (tile t of species s): the tile's particles are read
-// in chunks of kChunk; after one barrier per chunk (every load of the chunk
-// has landed) each particle is pushed, deposited into the tile's shared
-// accumulator, and written back: stayers compacted in place through a
-// shared cursor (a warp reserves its run with one shared atomic), movers
-// appended to their destination tile (one global atomic per distinct
-// destination per warp).  In-place writes of chunk k only touch slots below
-// the end of chunk k, all of which were read before the barrier.
+// Skeleton per block (tile t of species s): the tile's particles -- its main
+// region, then the arrivals the previous step left for it -- are read in
+// chunks of kChunk; after one barrier per chunk (every load of the chunk has
+// landed) each particle is pushed, deposited into the tile's shared
+// accumulator, and written back: stayers compacted in place at the front of
+// the main region through a shared cursor (a warp reserves its run with one
+// shared atomic), movers appended to their destination tile's arrivals in
+// the other buffer (one global atomic per distinct destination per warp).
+// In-place writes never pass the number of particles read, so they only
+// touch main-region slots already read or free.
 #pragma once
 #include "cpic_common.cuh"
 #include "cpic_bits.h"
@@ -749,8 +751,9 @@ k_push(const PushArgs a)
 	__shared__ __align__(8) uint64_t ebars[2];
 	__shared__ int s_cursor;
 	__shared__ int s_timeout;        // a bounded wait of this block expired
-	// base and capacity of the 3 x 3 tiles around this one: nearly every
-	// mover lands there, so its slot needs no dependent global loads
+	// arrivals base (in the buffer this step writes) and capacity of the
+	// 3 x 3 tiles around this one: nearly every mover lands there, so its
+	// slot needs no dependent global loads
 	__shared__ int64_t s_nbase[9];
 	__shared__ int32_t s_ncap[9];
 	const Grid &g = a.g;
@@ -784,17 +787,42 @@ k_push(const PushArgs a)
 
 	F::clear(fsm, W, g.tx);
 	const void *Etile = F::load_field(a, fsm, W, g.tx, tx0, ty0);
-	const int n = T.cnt[t];
+	// the chunks: the main region's particles, then the arrivals the
+	// previous step left in buffer r; a chunk never spans both, so every
+	// bulk copy starts on a 32-slot boundary
+	const int r = a.arr_r;
+	const int nm = T.cnt[t];
+	// (a count can pass the capacity: movers that found the region full
+	// went to the spill list but still took a slot number)
+	const int na = min(T.acnt[r][t], T.acap[t]);
 	const int64_t base = T.base[t];
-	const int nchunks = (n + kChunk - 1) / kChunk;
+	const int capt = T.cap[t];
+	const int64_t abase_r = T.abase[t] + (r ? T.abuf1 : 0);
+	const int64_t aofs_w = r ? 0 : T.abuf1;
+	int32_t *const acnt_w = T.acnt[r ^ 1];
+	const int nmc = (nm + kChunk - 1) / kChunk;
+	const int nchunks = nmc + (na + kChunk - 1) / kChunk;
+	auto chunk = [&](int ci, int64_t &first, int &len) {
+		if(ci < nmc)
+		{
+			first = base + (int64_t) ci * kChunk;
+			len = min(kChunk, nm - ci * kChunk);
+		}
+		else
+		{
+			const int o = (ci - nmc) * kChunk;
+			first = abase_r + o;
+			len = min(kChunk, na - o);
+		}
+	};
 	// neighbours are distinct tiles only with at least 3 tiles per side
 	const bool nb_ok = g.ntx >= 3 && g.nty >= 3;
 	if(threadIdx.x < 9 && nb_ok)
 	{
 		int dx = (int) threadIdx.x % 3 - 1, dy = (int) threadIdx.x / 3 - 1;
 		int nt = wrapn(tty + dy, g.nty) * g.ntx + wrapn(ttx + dx, g.ntx);
-		s_nbase[threadIdx.x] = T.base[nt];
-		s_ncap[threadIdx.x] = T.cap[nt];
+		s_nbase[threadIdx.x] = T.abase[nt] + aofs_w;
+		s_ncap[threadIdx.x] = T.acap[nt];
 	}
 	if(threadIdx.x == 0)
 	{
@@ -808,12 +836,19 @@ k_push(const PushArgs a)
 	}
 	__syncthreads();
 	if(threadIdx.x == 0 && nchunks > 0)
-		F::template stage_issue<kChunk>(a, s, base, min(kChunk, n), stage0, &bars[0]);
+	{
+		int64_t f0;
+		int l0;
+		chunk(0, f0, l0);
+		F::template stage_issue<kChunk>(a, s, f0, l0, stage0, &bars[0]);
+	}
 	const int lane = threadIdx.x & 31;
 
 	for(int ci = 0; ci < nchunks; ci++)
 	{
-		const int c0 = ci * kChunk;
+		int64_t cfirst;
+		int clen;
+		chunk(ci, cfirst, clen);
 		if(ci > 0 && ci % kCheckChunks == 0)
 		{
 			// every deposit of the previous chunks precedes the check (and
@@ -834,12 +869,16 @@ k_push(const PushArgs a)
 			if(ci >= 1 && !mbar_wait_bounded(&ebars[b], ((ci - 1) >> 1) & 1, a.status))
 				s_timeout = 1;
 			fence_proxy_async_smem();
-			F::template stage_issue<kChunk>(a, s, base + c0 + kChunk, min(kChunk, n - c0 - kChunk),
-					stage0 + b * sb, &bars[b]);
+			int64_t nf;
+			int nl;
+			chunk(ci + 1, nf, nl);
+			F::template stage_issue<kChunk>(a, s, nf, nl, stage0 + b * sb, &bars[b]);
 		}
-		// this chunk has landed: every global read of slots below
-		// c0 + kChunk is complete, so the in-place writes below are safe
-		// (the stayer cursor never passes the end of the chunks read)
+		// this chunk has landed: every global read of the main region's
+		// slots below the end of this chunk is complete, so the in-place
+		// writes below are safe (the stayer cursor never passes the number
+		// of particles read; past the main region's count it writes free
+		// slots, which nothing reads in this step)
 		if(!mbar_wait_bounded(&bars[ci & 1], (ci >> 1) & 1, a.status))
 			s_timeout = 1;
 		const unsigned char *buf = stage0 + (ci & 1) * sb;
@@ -852,7 +891,7 @@ k_push(const PushArgs a)
 		for(int k = 0; k < P; k++)
 		{
 			const int j = k * kPushThreads + threadIdx.x;
-			const bool valid = c0 + j < n;
+			const bool valid = j < clen;
 			if(valid)
 				rec[k] = F::template from_stage<kChunk>(buf, j, ids);
 			// the last record is in registers: this warp is done with the
@@ -876,7 +915,7 @@ k_push(const PushArgs a)
 			bs[k] = __ballot_sync(0xffffffffu, dest[k] == t);
 			// slots in the destination tiles: atomics issued now, their
 			// results consumed after the stayer writes
-			rv[k] = warp_reserve_issue(T.app, dest[k] >= 0 && dest[k] != t, dest[k]);
+			rv[k] = warp_reserve_issue(acnt_w, dest[k] >= 0 && dest[k] != t, dest[k]);
 		}
 		if(err) set_status(a.status, err);
 		// one shared-cursor reservation per warp for all its stayers
@@ -887,8 +926,11 @@ k_push(const PushArgs a)
 		if(lane == 0 && nst)
 			wb = atomicAdd(&s_cursor, nst);
 		wb = __shfl_sync(0xffffffffu, wb, 0);
+		// the main region holds this warp's stayers (else, rarely, the
+		// ones past its end take the spill list)
+		const bool room = wb + nst <= capt;
 		// one store per particle: its own tile's compacted prefix, or its
-		// slot in the destination tile, or the spill list
+		// slot in the destination tile's arrivals, or the spill list
 		#pragma unroll
 		for(int k = 0; k < P; k++)
 		{
@@ -896,8 +938,15 @@ k_push(const PushArgs a)
 			const bool move = dest[k] >= 0 && dest[k] != t;
 			const int slot = warp_reserve_finish(rv[k], move);
 			int64_t at = -1;
+			bool spill = false;
 			if(stay)
-				at = base + wb + __popc(bs[k] & lanemask_lt());
+			{
+				const int idx = wb + __popc(bs[k] & lanemask_lt());
+				if(room || idx < capt)
+					at = base + idx;
+				else
+					spill = true;
+			}
 			else if(move)
 			{
 				// the neighbour table covers the 3 x 3 tiles around this
@@ -917,20 +966,29 @@ k_push(const PushArgs a)
 				}
 				else
 				{
-					db = T.base[d];
-					dc = T.cap[d];
+					db = T.abase[d] + aofs_w;
+					dc = T.acap[d];
 				}
 				if(slot < dc)
 					at = db + slot;
 				else
+					spill = true;
+			}
+			if(spill)
+			{
+				double x, y, ux, uy;
+				F::to_spill_rec(rec[k], g, x, y, ux, uy);
+				// spill list full too: the particle stays in this tile,
+				// outside its cell's tile (every later pass handles that),
+				// until the host rebuilds the layout; with the main region
+				// full as well it is lost, and the status says so
+				if(!spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id))
 				{
-					double x, y, ux, uy;
-					F::to_spill_rec(rec[k], g, x, y, ux, uy);
-					// spill list full too: the particle stays in this
-					// tile, outside its cell's tile (every later pass
-					// handles that), until the host rebuilds the layout
-					if(!spill_push(a.spill_out[s], x, y, ux, uy, rec[k].id))
-						at = base + atomicAdd(&s_cursor, 1);
+					const int idx = atomicAdd(&s_cursor, 1);
+					if(idx < capt)
+						at = base + idx;
+					else
+						set_status(a.status, ST_SPILL_FULL);
 				}
 			}
 			if(at >= 0)
@@ -941,7 +999,10 @@ k_push(const PushArgs a)
 	__syncthreads();
 	if(threadIdx.x == 0)
 	{
-		T.stay[t] = s_cursor;
+		// the main region's count for the next step; this step's arrivals
+		// buffer is read and becomes the next step's buffer for movers
+		T.cnt[t] = min(s_cursor, capt);
+		T.acnt[r][t] = 0;
 		// after an expired wait a copy may still be landing in the stage:
 		// wait (bounded again) for the last one issued into each buffer
 		// before the block's shared memory is released
@@ -958,7 +1019,8 @@ k_push(const PushArgs a)
 
 // Generic pass over the spill list: records with no tile of their own
 // (the particle store overflowed).  E is read from global memory and the
-// deposit goes straight to global rho.  Records are placed in their tile
+// deposit goes straight to global rho.  Records are placed among their
+// tile's arrivals for the next step (the buffer this step's movers go to)
 // when it has room, else appended to spill_out.
 template <class F>
 __global__ void __launch_bounds__(kPushThreads)
@@ -986,11 +1048,13 @@ k_spill(const SpillArgs sa)
 				if(o.err) set_status(a.status, o.err);
 				F::deposit(a, s, nullptr, 0, 0, 0, 0, o);
 			}
-			int slot = warp_reserve(a.tiles[s].app, valid, o.dest);
+			const Tiles &T = a.tiles[s];
+			const int w = a.arr_r ^ 1;
+			int slot = warp_reserve(T.acnt[w], valid, o.dest);
 			if(valid)
 			{
-				if(slot < a.tiles[s].cap[o.dest])
-					F::store(a, s, a.tiles[s].base[o.dest] + slot, r);
+				if(slot < T.acap[o.dest])
+					F::store(a, s, T.abase[o.dest] + (w ? T.abuf1 : 0) + slot, r);
 				else
 				{
 					double x, y, ux, uy;
