@@ -94,34 +94,31 @@ struct cpic_ctx {
 
 // Moves the arrivals in buffer a.arr_r into each tile's main region, so that
 // every pass over the main regions sees all the species' particles (before a
-// host read, a rebuild or a re-layout); arrivals the main region has no room
-// for go to the spill list a.spill_out (cell units for the mixed form).
+// host read or a re-layout).  A tile whose main region has no room for all
+// of them keeps them where they are and is counted in *overflow (the host
+// then rebuilds the layout, which takes pending arrivals as they lie).
 template <class F>
-__global__ void k_merge(const PushArgs a)
+__global__ void k_merge(const PushArgs a, int32_t *overflow)
 {
 	const int s = blockIdx.y, t = blockIdx.x;
 	const Tiles &T = a.tiles[s];
 	const int r = a.arr_r;
 	const int na = min(T.acnt[r][t], T.acap[t]), nm = T.cnt[t];
-	const int k = min(na, max(0, T.cap[t] - nm));
+	if(na == 0)
+		return;
+	if(na > T.cap[t] - nm)
+	{
+		if(threadIdx.x == 0)
+			atomicAdd(overflow, 1);
+		return;
+	}
 	const int64_t src = T.abase[t] + (r ? T.abuf1 : 0), dst = T.base[t] + nm;
 	for(int i = threadIdx.x; i < na; i += blockDim.x)
-	{
-		typename F::Rec rec = F::load(a, s, src + i);
-		if(i < k)
-			F::store(a, s, dst + i, rec);
-		else
-		{
-			double x, y, ux, uy;
-			F::to_spill_rec(rec, a.g, x, y, ux, uy);
-			if(!spill_push(a.spill_out[s], x, y, ux, uy, rec.id))
-				set_status(a.status, ST_SPILL_FULL);
-		}
-	}
+		F::store(a, s, dst + i, F::load(a, s, src + i));
 	__syncthreads();
 	if(threadIdx.x == 0)
 	{
-		T.cnt[t] = nm + k;
+		T.cnt[t] = nm + na;
 		T.acnt[r][t] = 0;
 	}
 }
@@ -277,18 +274,29 @@ __global__ void k_rb_count(Grid g, Spill S, int64_t n, int32_t *newcnt)
 		atomicAdd(&newcnt[TileOf<F>::get(g, S, k)], 1);
 }
 
-// Copy each tile's particles from the old store to the new base.
+// Copy each tile's particles from the old store to the new base: its main
+// region, then its pending arrivals (buffer olda.arr_r).
 template <class F>
 __global__ void k_rb_copy(const PushArgs olda, const PushArgs newa, int s)
 {
-	int t = blockIdx.x;
-	int n = olda.tiles[s].cnt[t];
-	int64_t ob = olda.tiles[s].base[t], nb = newa.tiles[s].base[t];
-	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	const int t = blockIdx.x;
+	const Tiles &T = olda.tiles[s];
+	const int n = T.cnt[t];
+	const int na = min(T.acnt[olda.arr_r][t], T.acap[t]);
+	const int64_t ob = T.base[t], nb = newa.tiles[s].base[t];
+	const int64_t oab = T.abase[t] + (olda.arr_r ? T.abuf1 : 0);
+	for(int i = threadIdx.x; i < n + na; i += blockDim.x)
 	{
-		typename F::Rec r = F::load(olda, s, ob + i);
+		typename F::Rec r = F::load(olda, s, i < n ? ob + i : oab + (i - n));
 		F::store(newa, s, nb + i, r);
 	}
+}
+
+// Particles of each tile: its main region's and its pending arrivals.
+__global__ void k_tile_total(int nt, const Tiles T, int abuf, int32_t *out)
+{
+	for(int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x)
+		out[t] = T.cnt[t] + min(T.acnt[abuf][t], T.acap[t]);
 }
 
 template <class F>
@@ -974,7 +982,7 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	if(fresh)
 		CK(cudaMemsetAsync(newcnt, 0, nt * sizeof(int32_t), st));
 	else
-		CK(cudaMemcpyAsync(newcnt, S.tiles.cnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+		k_tile_total<<<grid_blocks(nt), 256, 0, st>>>(nt, S.tiles, c->spill_cur, newcnt);
 	bool mix = c->precision == CPIC_MIXED;
 	// the upload of a species: one conversion pass (records, keys and the
 	// histogram of (tile, sign of ux)), then two sorting passes below
@@ -1074,10 +1082,11 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	newa.tiles[s].cap = ncap;
 	newa.f64[s] = S.f64_alt;
 	newa.mix[s] = S.mix_alt;
+	// the spill records go after each tile's copied particles
 	if(fresh)
 		CK(cudaMemsetAsync(fill, 0, nt * sizeof(int32_t), st));
 	else
-		CK(cudaMemcpyAsync(fill, S.tiles.cnt, nt * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+		k_tile_total<<<grid_blocks(nt), 256, 0, st>>>(nt, S.tiles, c->spill_cur, fill);
 	if(!fresh)
 	{
 		if(mix) launch_rb_copy<Mix>(olda, newa, s, nt, st);
@@ -1171,53 +1180,45 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	return CPIC_OK;
 }
 
-// Every species' pending arrivals (buffer spill_cur) into the main regions,
-// overflow to spill[spill_cur] (the list the next stage and a rebuild read).
-static int merge_arrivals(cpic_ctx *c)
+// Every species' pending arrivals (buffer spill_cur) into the main regions
+// where they fit; returns in *unmerged the number of tiles where they did
+// not (synchronises the context's stream).
+static int merge_arrivals(cpic_ctx *c, int32_t *unmerged)
 {
+	*unmerged = 0;
 	if(c->nspecies == 0) return CPIC_OK;
 	PushArgs a = make_args(c, c->spill_cur);
-	for(int s = 0; s < c->nspecies; s++)
-		a.spill_out[s] = c->sp[s].spill[c->spill_cur];
+	CK(cudaMemsetAsync(c->counter, 0, sizeof(int32_t), c->stream));
 	dim3 grid(c->ntiles, c->nspecies);
 	if(c->precision == CPIC_MIXED)
-		k_merge<Mix><<<grid, 256, 0, c->stream>>>(a);
+		k_merge<Mix><<<grid, 256, 0, c->stream>>>(a, c->counter);
 	else
-		k_merge<F64><<<grid, 256, 0, c->stream>>>(a);
+		k_merge<F64><<<grid, 256, 0, c->stream>>>(a, c->counter);
 	CK(cudaGetLastError());
+	CK(cudaMemcpyAsync(unmerged, c->counter, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
 	return CPIC_OK;
 }
 
 // After the context's stream has been synchronised: rebuilds the layout of
-// every species whose spill list holds records (merging the pending arrivals
-// first, since a rebuild reads the main regions and the spill list).
+// every species whose spill list holds records (a rebuild takes the main
+// regions, the pending arrivals and the spill list).
 static int rebuild_if_spilled(cpic_ctx *c)
 {
 	c->last_spill = 0;
-	bool any = false;
 	for(int s = 0; s < c->nspecies; s++)
 	{
 		int32_t ns = 0;
 		CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
 				cudaMemcpyDeviceToHost));
 		c->last_spill += ns;
-		any = any || ns > 0;
-	}
-	if(!any) return CPIC_OK;
-	int r = merge_arrivals(c);
-	if(r) return r;
-	CK(cudaStreamSynchronize(c->stream));
-	for(int s = 0; s < c->nspecies; s++)
-	{
-		int32_t ns = 0;
-		CK(cudaMemcpy(&ns, c->sp[s].spill[c->spill_cur].count, sizeof(int32_t),
-				cudaMemcpyDeviceToHost));
 		if(ns > 0)
 		{
 			// a tile overflowed: more headroom from now on
 			c->rebuilds++;
 			c->slack_pct = std::min(200, 2 * c->slack_pct);
-			if((r = rebuild_species(c, s, false, nullptr, 0))) return r;
+			int r = rebuild_species(c, s, false, nullptr, 0);
+			if(r) return r;
 		}
 	}
 	return CPIC_OK;
@@ -1302,10 +1303,21 @@ static int plasma_stage_async(cpic_ctx *c, bool deposit_only, cudaEvent_t ev0 = 
 // overflowed).
 static int normalize(cpic_ctx *c)
 {
-	int r = merge_arrivals(c);
-	if(r) return r;
 	CK(cudaStreamSynchronize(c->stream));
-	return rebuild_if_spilled(c);
+	int r = rebuild_if_spilled(c);
+	if(r) return r;
+	int32_t unmerged = 0;
+	if((r = merge_arrivals(c, &unmerged))) return r;
+	// arrivals that did not fit their tile's main region: a new layout
+	// (the main regions full: more headroom from now on)
+	if(unmerged > 0)
+	{
+		c->rebuilds++;
+		c->slack_pct = std::min(200, 2 * c->slack_pct);
+		for(int s = 0; s < c->nspecies; s++)
+			if((r = rebuild_species(c, s, false, nullptr, 0))) return r;
+	}
+	return CPIC_OK;
 }
 
 static int field_stage_async(cpic_ctx *c)
@@ -1637,6 +1649,22 @@ CPIC_API int cpic_add_species(cpic_ctx_t *c, double q, double m, int64_t n,
 	memset((void *) &S, 0, sizeof(S));
 	S.q = q; S.m = m; S.n = n;
 	S.vmax = vmax;
+	// the fused kernel's instance when the caller left it to the library:
+	// 1 particle per thread (chunks of 256) while every species has fewer
+	// than kSmallTile particles per tile, else 2 (chunks of 512).  A tile's
+	// last main-region chunk and its arrivals chunk are partial, and on
+	// small tiles they and the latency between chunks dominate: the FP64
+	// two-species 512x512 workload (about 1,100 particles per 8x8 tile and
+	// species) steps in 1.498 ms with 1, 1.678 ms with 2; two-stream 2048x2048
+	// (102,400 per tile) is fastest with 2.
+	if(c->p.particles_per_thread <= 0)
+	{
+		constexpr int64_t kSmallTile = 4096;
+		bool small = n / std::max(1, c->ntiles) < kSmallTile;
+		for(int k = 0; k < c->nspecies; k++)
+			small = small && c->sp[k].n / std::max(1, c->ntiles) < kSmallTile;
+		c->ppt = small ? 1 : kPPT;
+	}
 	int nt = c->ntiles;
 	CK(cudaMalloc(&S.tiles.base, nt * sizeof(int64_t)));
 	CK(cudaMalloc(&S.tiles.cap, nt * sizeof(int32_t)));

@@ -66,7 +66,9 @@ typedef struct cpic_params {
 	                          * nx and ny; 0 = auto */
 	int32_t halo;            /* deposit halo in cells; 0 = auto */
 	int32_t track_ids;       /* keep a particle id per particle (MIXED) */
-	int32_t particles_per_thread; /* fused kernel instance: 1, 2 or 4; 0 = 2 */
+	int32_t particles_per_thread; /* fused kernel instance: 1, 2 or 4; 0 = chosen
+	                               * at cpic_add_species: 1 while every species
+	                               * has < 4096 particles per tile, else 2 */
 	int32_t reserved[6];
 } cpic_params_t;
 
