@@ -48,6 +48,11 @@ WORKLOADS = {
                        "two-stream 512x512, 100 electrons/cell (26,214,400), beams +-0.2, vth 0.01, "
                        "amp 0.01, dt 0.05"),
     "two_stream_64": (64, 100, 0.2, 0.01, 0.01, "two-stream 64x64, 100 electrons/cell (409,600)"),
+    # a grid whose side is not a power of two (1920 = 2^7 3 5: mixed-radix field
+    # solve, compare-wrapped cells) with the benchmark's 32x32 tiles
+    "two_stream_1920": (1920, 100, 0.2, 0.01, 0.01,
+                        "two-stream 1920x1920, 100 electrons/cell (368,640,000), beams +-0.2, "
+                        "vth 0.01, amp 0.01, dt 0.05"),
 }
 
 
