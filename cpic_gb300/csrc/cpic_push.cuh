@@ -528,12 +528,18 @@ struct Mix {
 		float vpy = __fmaf_rn(-vmx, sp.tz_f, vmy);
 		float ux = __fadd_rn(__fmaf_rn(vpy, sp.sz_f, vmx), hx);
 		float uy = __fadd_rn(__fmaf_rn(-vpx, sp.sz_f, vmy), hy);
-		if(fabsf(ux) > sp.umax_x_f || fabsf(uy) > sp.umax_y_f)
-			o.err |= ST_UMAX;
-		if(!isfinite(ux) || !isfinite(uy))
+		// one compare per component on the common path: a NaN fails
+		// |u| <= umax as an out-of-range speed does (0.9 % of the kernel's
+		// time against four compares)
+		if(!(fabsf(ux) <= sp.umax_x_f) || !(fabsf(uy) <= sp.umax_y_f))
 		{
-			o.err |= ST_NAN;
-			ux = 0.0f; uy = 0.0f;
+			if(fabsf(ux) > sp.umax_x_f || fabsf(uy) > sp.umax_y_f)
+				o.err |= ST_UMAX;
+			if(!isfinite(ux) || !isfinite(uy))
+			{
+				o.err |= ST_NAN;
+				ux = 0.0f; uy = 0.0f;
+			}
 		}
 		int sx = 0, sy = 0;
 		if(a.iter != 0)
