@@ -309,7 +309,7 @@ struct F64 {
 			return;
 		}
 		int lx = o.rx + H, ly = o.ry + H;
-		if(sm && lx >= 0 && ly >= 0 && lx + 1 < W && ly + 1 < W)
+		if(sm && (unsigned) lx < (unsigned) (W - 1) && (unsigned) ly < (unsigned) (W - 1))
 		{
 			long long *p = reinterpret_cast<long long *>(sm) + ly * W + lx;
 			long long *q = p + W * W;
@@ -650,7 +650,7 @@ struct Mix {
 			int W, int H, int tx0, int ty0, const Out &o)
 	{
 		int lx = o.rx + H, ly = o.ry + H;
-		if(sm && lx >= 0 && ly >= 0 && lx + 1 < W && ly + 1 < W)
+		if(sm && (unsigned) lx < (unsigned) (W - 1) && (unsigned) ly < (unsigned) (W - 1))
 		{
 			uint32_t *p = sh32(sm, W, a.g.tx) + ly * W + lx;
 			atomicAdd(&p[0], o.wq[0]);
