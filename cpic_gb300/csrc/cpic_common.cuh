@@ -67,10 +67,11 @@ struct StoreF64 {
 	int32_t *id;
 };
 
+// The mixed form keeps each particle's four floats together (one 16-byte
+// load or store each), its packed cell in a column of its own.
 struct StoreMix {
-	int32_t *cell;   // iy * nx + ix
-	float *ox, *oy;  // offset inside the cell, [0, 1)
-	float *ux, *uy;  // physical velocity
+	int32_t *cell;   // (cy << lcx) + cx
+	float4 *ou;      // (ox, oy, ux, uy): offset inside the cell in [0, 1), velocity
 	int32_t *id;     // optional (nullptr when ids are not tracked)
 };
 

@@ -884,10 +884,7 @@ static int alloc_store(cpic_ctx *c, SpeciesHost &S, int64_t cap, bool alt)
 	{
 		StoreMix &st = alt ? S.mix_alt : S.mix;
 		CK(cudaMalloc(&st.cell, nal * sizeof(int32_t)));
-		CK(cudaMalloc(&st.ox, nal * sizeof(float)));
-		CK(cudaMalloc(&st.oy, nal * sizeof(float)));
-		CK(cudaMalloc(&st.ux, nal * sizeof(float)));
-		CK(cudaMalloc(&st.uy, nal * sizeof(float)));
+		CK(cudaMalloc(&st.ou, nal * sizeof(float4)));
 		st.id = nullptr;
 		if(c->p.track_ids)
 			CK(cudaMalloc(&st.id, nal * sizeof(int32_t)));
@@ -906,7 +903,7 @@ static void free_store(cpic_ctx *c, SpeciesHost &S, bool alt)
 	else
 	{
 		StoreMix &st = alt ? S.mix_alt : S.mix;
-		cudaFree(st.cell); cudaFree(st.ox); cudaFree(st.oy); cudaFree(st.ux); cudaFree(st.uy);
+		cudaFree(st.cell); cudaFree(st.ou);
 		cudaFree(st.id);
 		memset(&st, 0, sizeof(st));
 	}
@@ -1061,7 +1058,7 @@ static int rebuild_species(cpic_ctx *c, int s, bool fresh, const Spill *staging,
 	const int64_t slots = total + 2 * atotal;
 
 	// the alternate store receives the new layout
-	bool have_alt = mix ? S.mix_alt.ux != nullptr : S.f64_alt.ux != nullptr;
+	bool have_alt = mix ? S.mix_alt.ou != nullptr : S.f64_alt.ux != nullptr;
 	if(S.cap_alt < slots || !have_alt)
 	{
 		free_store(c, S, true);

@@ -87,7 +87,8 @@ __global__ void k_gather_mix(Grid g, StoreMix st, const int64_t *base, const int
 		int cx = c & ((1 << g.lcx) - 1), cy = c >> g.lcx;
 		int x1 = cx + 1 == g.nx ? 0 : cx + 1;
 		int y1 = cy + 1 == g.ny ? 0 : cy + 1;
-		float ox = st.ox[b + i], oy = st.oy[b + i];
+		const float4 v = st.ou[b + i];
+		float ox = v.x, oy = v.y;
 		float dxo = 1.0f - ox, dyo = 1.0f - oy;
 		float2 e00 = E[(int64_t) cy * g.nx + cx], e01 = E[(int64_t) y1 * g.nx + cx];
 		float2 e10 = E[(int64_t) cy * g.nx + x1], e11 = E[(int64_t) y1 * g.nx + x1];

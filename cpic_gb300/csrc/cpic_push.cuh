@@ -405,8 +405,8 @@ struct Mix {
 		const StoreMix &st = a.mix[s];
 		Rec r;
 		r.cell = st.cell[i];
-		r.ox = st.ox[i]; r.oy = st.oy[i];
-		r.ux = st.ux[i]; r.uy = st.uy[i];
+		const float4 v = st.ou[i];
+		r.ox = v.x; r.oy = v.y; r.ux = v.z; r.uy = v.w;
 		r.id = st.id ? st.id[i] : 0;
 		return r;
 	}
@@ -415,8 +415,7 @@ struct Mix {
 	{
 		const StoreMix &st = a.mix[s];
 		st.cell[i] = r.cell;
-		st.ox[i] = r.ox; st.oy[i] = r.oy;
-		st.ux[i] = r.ux; st.uy[i] = r.uy;
+		st.ou[i] = make_float4(r.ox, r.oy, r.ux, r.uy);
 		if(st.id) st.id[i] = r.id;
 	}
 
@@ -427,13 +426,13 @@ struct Mix {
 	{
 		const StoreMix &st = a.mix[s];
 		st.cell[i] = r.cell;
-		st.ox[i] = r.ox; st.oy[i] = r.oy;
-		st.ux[i] = r.ux; st.uy[i] = r.uy;
+		st.ou[i] = make_float4(r.ox, r.oy, r.ux, r.uy);
 		if(kIds) st.id[i] = r.id;
 	}
 
-	// Staged chunk layout: cell, ox, oy, ux, uy (C 32-bit words each)
-	// and, when ids are tracked, id, for a chunk of C particles.
+	// Staged chunk layout: cell (C 32-bit words), the (ox, oy, ux, uy)
+	// quadruples (C x 16 bytes) and, when ids are tracked, id, for a chunk
+	// of C particles.
 	static __host__ __device__ __forceinline__ size_t stage_bytes(bool ids, int C)
 	{
 		return (size_t) C * 4 * (ids ? 6 : 5);
@@ -445,12 +444,10 @@ struct Mix {
 	{
 		const StoreMix &st = a.mix[s];
 		uint32_t b4 = (uint32_t) ((cnt * 4 + 15) & ~15);
-		mbar_arrive_expect_tx(bar, (st.id ? 6 : 5) * b4);
+		uint32_t b16 = (uint32_t) cnt * 16;
+		mbar_arrive_expect_tx(bar, (st.id ? 2 : 1) * b4 + b16);
 		bulk_g2s(buf, st.cell + first, b4, bar);
-		bulk_g2s(buf + C * 4, st.ox + first, b4, bar);
-		bulk_g2s(buf + C * 8, st.oy + first, b4, bar);
-		bulk_g2s(buf + C * 12, st.ux + first, b4, bar);
-		bulk_g2s(buf + C * 16, st.uy + first, b4, bar);
+		bulk_g2s(buf + C * 4, st.ou + first, b16, bar);
 		if(st.id)
 			bulk_g2s(buf + C * 20, st.id + first, b4, bar);
 	}
@@ -458,11 +455,10 @@ struct Mix {
 	template <int C>
 	static __device__ __forceinline__ Rec from_stage(const unsigned char *buf, int j, bool ids)
 	{
-		const float *f = reinterpret_cast<const float *>(buf);
 		Rec r;
 		r.cell = reinterpret_cast<const int32_t *>(buf)[j];
-		r.ox = f[C + j]; r.oy = f[2 * C + j];
-		r.ux = f[3 * C + j]; r.uy = f[4 * C + j];
+		const float4 v = reinterpret_cast<const float4 *>(buf + C * 4)[j];
+		r.ox = v.x; r.oy = v.y; r.ux = v.z; r.uy = v.w;
 		r.id = ids ? reinterpret_cast<const int32_t *>(buf)[5 * C + j] : 0;
 		return r;
 	}
