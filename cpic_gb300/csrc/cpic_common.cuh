@@ -289,7 +289,7 @@ frame_node(const Grid &g, int W, int H, int tx0, int ty0, int i)
 struct Resv { int leader, rank, own; };
 
 __device__ __forceinline__ Resv
-warp_reserve_issue(int32_t *app, bool move, int dest)
+warp_reserve_issue(int32_t *cnt, bool move, int dest)
 {
 	Resv r;
 	const unsigned grp = __match_any_sync(0xffffffffu, move ? dest : -1);
@@ -297,7 +297,7 @@ warp_reserve_issue(int32_t *app, bool move, int dest)
 	r.rank = __popc(grp & lanemask_lt());
 	r.own = 0;
 	if(move && r.rank == 0)
-		r.own = atomicAdd(&app[dest], __popc(grp));
+		r.own = atomicAdd(&cnt[dest], __popc(grp));
 	return r;
 }
 
@@ -312,9 +312,9 @@ warp_reserve_finish(const Resv &r, bool move)
 // destination tile in the warp.  Must be called by the whole warp; returns
 // the slot within the destination tile for lanes with `move`, else -1.
 __device__ __forceinline__ int
-warp_reserve(int32_t *app, bool move, int dest)
+warp_reserve(int32_t *cnt, bool move, int dest)
 {
-	return warp_reserve_finish(warp_reserve_issue(app, move, dest), move);
+	return warp_reserve_finish(warp_reserve_issue(cnt, move, dest), move);
 }
 
 // ------------------------------------------------ bulk copies (TMA engine)
