@@ -218,11 +218,13 @@ struct F64 {
 			y += uy * a.dt;
 		}
 		// periodic_boundary_ppack, comm_plasma.c:725-747 (X then Y; the
-		// compares on the integer pipe, cpic_bits.h)
-		if(bits::ge_pos(x, g.Lx)) x -= g.Lx;
-		else if(bits::lt_zero(x)) x += g.Lx;
-		if(bits::ge_pos(y, g.Ly)) y -= g.Ly;
-		else if(bits::lt_zero(y)) y += g.Ly;
+		// compares on the integer pipe, cpic_bits.h).  A branch around the
+		// rare wrap: computed for every particle and selected, the two
+		// additions took 4 % of the FP64 form's time.
+		if(__builtin_expect(bits::ge_pos(x, g.Lx) || bits::lt_zero(x), 0))
+			x = bits::ge_pos(x, g.Lx) ? x - g.Lx : x + g.Lx;
+		if(__builtin_expect(bits::ge_pos(y, g.Ly) || bits::lt_zero(y), 0))
+			y = bits::ge_pos(y, g.Ly) ? y - g.Ly : y + g.Ly;
 		if(!bits::is_finite(x) || !bits::is_finite(y))
 		{
 			o.err |= ST_NAN;
