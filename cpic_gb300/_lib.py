@@ -85,6 +85,7 @@ SIGNATURES = [
     ("cpic_time_steps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, D, D, D]),
     ("cpic_tile_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
     ("cpic_layout_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    ("cpic_field_tile_copy", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
     ("cpic_poisson_noalloc", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                             ctypes.c_int64, ctypes.c_void_p]),
     ("cpic_ensemble_create", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
@@ -294,6 +295,12 @@ class Context:
         out = (ctypes.c_int64 * 4)()
         self._check(self.lib.cpic_layout_stats(self.h, out), "cpic_layout_stats")
         return dict(last_spill=out[0], rebuilds=out[1], slack_pct=out[2], blocks_per_sm=out[3])
+
+    def field_tile_copy(self):
+        """1 when the fused kernel copies field tiles with 2D tensor copies."""
+        out = ctypes.c_int32()
+        self._check(self.lib.cpic_field_tile_copy(self.h, ctypes.byref(out)), "cpic_field_tile_copy")
+        return out.value
 
     def tile_info(self):
         out = (ctypes.c_int32 * 4)()

@@ -24,6 +24,7 @@
 // species charge multiplies the tile sums at the flush.
 #pragma once
 #include <cstdint>
+#include <cuda.h>            // CUtensorMap (the type only; no driver library is linked)
 #include <cuda_runtime.h>
 #include "cpic_bits.h"
 
@@ -135,6 +136,12 @@ struct SpeciesStep {
 };
 
 struct PushArgs {
+	// mixed form: 2D tensor map of E32 (nx x ny elements of 8 bytes, box
+	// (tx + 2) x (ty + 1)) for the fused kernel's field tile; valid when
+	// emap_ok.  Kept in the kernel's parameter space, where the tensor
+	// copy reads it.
+	CUtensorMap emap;
+	int emap_ok;
 	Grid g;
 	int nspecies;
 	int arr_r;           // arrivals buffer read by this step (movers go to 1 - arr_r)
@@ -356,6 +363,18 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 {
 	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
 			:: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+// A 2D tile of a tensor map (box dimensions in the map) into shared
+// memory; x, y the box's first element and row.  dst 128-byte aligned; x
+// times the element size a multiple of 16 bytes.
+__device__ __forceinline__ void tensor_g2s_2d(void *dst, const CUtensorMap *map, int x, int y,
+		uint64_t *bar)
+{
+	asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+			" [%0], [%1, {%2, %3}], [%4];"
+			:: "r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y),
+			"r"(smem_addr(bar)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)

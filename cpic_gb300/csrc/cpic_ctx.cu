@@ -12,6 +12,7 @@
 #include <vector>
 #include <algorithm>
 #include <mutex>
+#include <cudaTypedefs.h>   // PFN_cuTensorMapEncodeTiled
 
 #include "../../include/cpic_gpu.h"
 #include "cpic_common.cuh"
@@ -88,6 +89,8 @@ struct cpic_ctx {
 	size_t scratch_n;
 	int32_t *counter;         // device scalar
 	int32_t *probe_h;         // pinned: status word and each species' spill count
+	CUtensorMap emap;         // mixed form: E32 as 2D tiles for the fused kernel
+	bool emap_ok;
 	unsigned long long *counter_pair;  // two device scalars (upload check)
 };
 
@@ -798,7 +801,49 @@ static PushArgs make_args(cpic_ctx *c, int cur_spill)
 	a.Ey64 = c->Ey64;
 	a.E32 = c->precision == CPIC_MIXED ? c->E32 : nullptr;
 	a.status = c->status;
+	if(c->emap_ok)
+	{
+		a.emap = c->emap;
+		a.emap_ok = 1;
+	}
 	return a;
+}
+
+// The mixed form's field tiles as 2D tensor copies: a map of E32 (nx x ny
+// elements of 8 bytes, row pitch nx * 8) with a box of (tx + 2) x (ty + 1)
+// elements, the tile's (tx + 1) x (ty + 1) nodes padded to an even width.
+// The copy engine wants the box's row and its first column on 16-byte
+// boundaries (tx even: tile origins and the box width are even), the row
+// pitch a multiple of 16 bytes (nx even), at most 256 elements per box
+// side and a 128-byte aligned destination (every staged chunk size is a
+// multiple of 128 bytes).  Otherwise, or without the driver's encoder,
+// the fused kernel loads field tiles by threads.
+static bool encode_field_map(cpic_ctx *c)
+{
+	const Grid &g = c->g;
+	if(c->precision != CPIC_MIXED || g.tx % 2 || g.nx % 2 || g.tx + 2 > 256 || g.ty + 1 > 256)
+		return false;
+	for(int P : kPPTChoices)
+		for(int ids = 0; ids < 2; ids++)
+			if(Mix::stage_bytes(ids != 0, chunk_of(P)) % 128)
+				return false;
+	static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+		void *fn = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+				&q) != cudaSuccess || q != cudaDriverEntryPointSuccess)
+			fn = nullptr;
+		return (PFN_cuTensorMapEncodeTiled_v12000) fn;
+	}();
+	if(!encode)
+		return false;
+	const cuuint64_t dims[2] = {(cuuint64_t) g.nx, (cuuint64_t) g.ny};
+	const cuuint64_t pitch[1] = {(cuuint64_t) g.nx * sizeof(float2)};
+	const cuuint32_t box[2] = {(cuuint32_t) (g.tx + 2), (cuuint32_t) (g.ty + 1)};
+	const cuuint32_t step[2] = {1, 1};
+	return encode(&c->emap, CU_TENSOR_MAP_DATA_TYPE_INT64, 2, c->E32, dims, pitch, box, step,
+			CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+			CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 static void fill_species_step(cpic_ctx *c, PushArgs &a, int64_t iter)
@@ -1514,6 +1559,7 @@ CPIC_API int cpic_create(const cpic_params_t *p, cpic_ctx_t **out)
 		AL(c->twx32, g.nx * sizeof(float2));
 		AL(c->twy32, g.ny * sizeof(float2));
 		cudaMemset(c->E32, 0, ng * sizeof(float2));
+		c->emap_ok = encode_field_map(c);
 	}
 #undef AL
 	cudaMemset(c->rho, 0, ng * sizeof(long long));
@@ -2214,6 +2260,13 @@ CPIC_API int cpic_layout_stats(const cpic_ctx_t *c, int64_t *out)
 		else
 			out[3] = push_f64_blocks_per_sm(push_smem(c), c->ppt);
 	}
+	return CPIC_OK;
+}
+
+CPIC_API int cpic_field_tile_copy(const cpic_ctx_t *c, int32_t *mode)
+{
+	if(!c || !mode) return CPIC_EINVAL;
+	*mode = c->emap_ok ? 1 : 0;
 	return CPIC_OK;
 }
 

@@ -347,6 +347,15 @@ struct F64 {
 		return nullptr;
 	}
 
+	// the FP64 form reads E from global memory: no field tile to copy
+	static __device__ __forceinline__ bool field_tma(const PushArgs &, int, int) { return false; }
+	static __device__ __forceinline__ const void *field_tile(unsigned char *) { return nullptr; }
+	static __device__ __forceinline__ const void *field_issue(const PushArgs &, unsigned char *,
+			int, int, uint64_t *)
+	{
+		return nullptr;
+	}
+
 	static __device__ __forceinline__ Rec from_spill(const Spill &S, int64_t k, const Grid &)
 	{
 		Rec r;
@@ -395,11 +404,12 @@ struct Mix {
 		uint32_t err;
 	};
 
-	// shared memory: the (T+1) x (T+1) E tile, then the W x W u32
-	// accumulator
+	// shared memory: the E tile, T + 1 rows of T + 1 nodes with a row
+	// pitch of T + 2 (the tensor copy's box is an even number of 8-byte
+	// elements wide), then the W x W u32 accumulator
 	static __host__ __device__ size_t smem_bytes(int W, int T)
 	{
-		return (size_t) W * W * sizeof(uint32_t) + (size_t) (T + 1) * (T + 1) * sizeof(float2);
+		return (size_t) W * W * sizeof(uint32_t) + (size_t) (T + 2) * (T + 1) * sizeof(float2);
 	}
 
 	static __device__ __forceinline__ Rec load(const PushArgs &a, int s, int64_t i)
@@ -473,8 +483,8 @@ struct Mix {
 		return __float_as_uint(f) - 0x4B000000u;
 	}
 
-	// Etile: (T+1) x (T+1) shared tile of E at the tile's nodes, or null
-	// for the global field (spill records).
+	// Etile: shared tile of E at the tile's (T+1) x (T+1) nodes (row pitch
+	// T + 2), or null for the global field (spill records).
 	template <bool GP2 = true>
 	static __device__ __forceinline__ Out push(const PushArgs &a, int s, Rec &r,
 			int tx0, int ty0, const void *Etile)
@@ -498,7 +508,7 @@ struct Mix {
 		if(Etile && (unsigned) lx < (unsigned) g.tx && (unsigned) ly < (unsigned) g.ty)
 		{
 			const float2 *Et = (const float2 *) Etile;
-			int W = g.tx + 1;
+			int W = g.tx + 2;
 			const float2 *p = Et + ly * W + lx;
 			e00 = p[0]; e01 = p[W]; e10 = p[1]; e11 = p[W + 1];
 		}
@@ -586,14 +596,14 @@ struct Mix {
 		return o;
 	}
 
-	// Shared layout: [float2 E tile (T+1)^2][u32 accumulator W*W].
+	// Shared layout: [float2 E tile (T+1) x (T+2)][u32 accumulator W*W].
 	static __device__ __forceinline__ float2 *shE(unsigned char *sm, int)
 	{
 		return reinterpret_cast<float2 *>(sm);
 	}
 	static __device__ __forceinline__ uint32_t *sh32(unsigned char *sm, int, int T)
 	{
-		return reinterpret_cast<uint32_t *>(sm + (size_t) (T + 1) * (T + 1) * 8);
+		return reinterpret_cast<uint32_t *>(sm + (size_t) (T + 2) * (T + 1) * 8);
 	}
 
 	static __device__ __forceinline__ void clear(unsigned char *sm, int W, int T)
@@ -678,18 +688,45 @@ struct Mix {
 		}
 	}
 
+	// The field tile by per-thread loads (nodes past the grid's last row
+	// or column wrap to the first).
 	static __device__ __forceinline__ const void *load_field(const PushArgs &a, unsigned char *sm,
 			int W, int T, int tx0, int ty0)
 	{
 		const Grid &g = a.g;
 		float2 *Et = shE(sm, W);
-		int WE = g.tx + 1;
+		const int WE = g.tx + 1;
 		for(int i = threadIdx.x; i < WE * (g.ty + 1); i += blockDim.x)
 		{
 			int lx = i % WE, ly = i / WE;
 			int gx = wrapn(tx0 + lx, g.nx), gy = wrapn(ty0 + ly, g.ny);
-			Et[i] = a.E32[(int64_t) gy * g.nx + gx];
+			Et[ly * (g.tx + 2) + lx] = a.E32[(int64_t) gy * g.nx + gx];
 		}
+		return Et;
+	}
+
+	// Whether this tile's field comes by one 2D tensor copy: a map exists
+	// (tiles of an even width, so the box starts on a 16-byte boundary)
+	// and the tile is not in the grid's last column or row, whose nodes
+	// wrap (those tiles load by threads).  The box's extra column is read
+	// and never used.
+	static __device__ __forceinline__ bool field_tma(const PushArgs &a, int tx0, int ty0)
+	{
+		return a.emap_ok && tx0 + a.g.tx < a.g.nx && ty0 + a.g.ty < a.g.ny;
+	}
+
+	static __device__ __forceinline__ const void *field_tile(unsigned char *sm)
+	{
+		return shE(sm, 0);
+	}
+
+	// Thread 0: arm bar with the box's bytes and copy the tile's field.
+	static __device__ __forceinline__ const void *field_issue(const PushArgs &a, unsigned char *sm,
+			int tx0, int ty0, uint64_t *bar)
+	{
+		float2 *Et = shE(sm, 0);
+		mbar_arrive_expect_tx(bar, (uint32_t) ((a.g.tx + 2) * (a.g.ty + 1) * sizeof(float2)));
+		tensor_g2s_2d(Et, &a.emap, tx0, ty0, bar);
 		return Et;
 	}
 
@@ -745,7 +782,7 @@ struct Mix {
 // GP2: nx and ny are powers of two (the mixed form wraps cells with a mask).
 template <class F, int MinBlocks = F::kMinBlocks, bool Ids = true, int P = kPPT, bool GP2 = true>
 __global__ void __launch_bounds__(kPushThreads, MinBlocks)
-k_push(const PushArgs a)
+k_push(const __grid_constant__ PushArgs a)
 {
 	constexpr int kChunk = chunk_of(P);
 	constexpr int kCheckChunks = check_chunks(P);
@@ -753,6 +790,7 @@ k_push(const PushArgs a)
 	extern __shared__ __align__(128) unsigned char smem[];
 	__shared__ __align__(8) uint64_t bars[2];
 	__shared__ __align__(8) uint64_t ebars[2];
+	__shared__ __align__(8) uint64_t fbar;   // the field tile's tensor copy
 	__shared__ int s_cursor;
 	__shared__ int s_timeout;        // a bounded wait of this block expired
 	// arrivals base (in the buffer this step writes) and capacity of the
@@ -790,7 +828,10 @@ k_push(const PushArgs a)
 	unsigned char *fsm = stage0 + 2 * sb;
 
 	F::clear(fsm, W, g.tx);
-	const void *Etile = F::load_field(a, fsm, W, g.tx, tx0, ty0);
+	// the field tile: one 2D tensor copy (issued with the barriers below)
+	// where the form has a map for it, else per-thread loads
+	const bool ftma = F::field_tma(a, tx0, ty0);
+	const void *Etile = ftma ? F::field_tile(fsm) : F::load_field(a, fsm, W, g.tx, tx0, ty0);
 	// the chunks: the main region's particles, then the arrivals the
 	// previous step left in buffer r; a chunk never spans both, so every
 	// bulk copy starts on a 32-slot boundary
@@ -836,7 +877,10 @@ k_push(const PushArgs a)
 		mbar_init(&bars[1], 1);
 		mbar_init(&ebars[0], kPushThreads / 32);   // "empty": one per warp
 		mbar_init(&ebars[1], kPushThreads / 32);
+		mbar_init(&fbar, 1);
 		fence_mbar_init();
+		if(ftma)
+			F::field_issue(a, fsm, tx0, ty0, &fbar);
 	}
 	__syncthreads();
 	if(threadIdx.x == 0 && nchunks > 0)
@@ -847,6 +891,8 @@ k_push(const PushArgs a)
 		F::template stage_issue<kChunk>(a, s, f0, l0, stage0, &bars[0]);
 	}
 	const int lane = threadIdx.x & 31;
+	if(ftma && !mbar_wait_bounded(&fbar, 0, a.status))
+		s_timeout = 1;
 
 	for(int ci = 0; ci < nchunks; ci++)
 	{
@@ -1011,12 +1057,16 @@ k_push(const PushArgs a)
 		// wait (bounded again) for the last one issued into each buffer
 		// before the block's shared memory is released
 		if(s_timeout)
+		{
 			for(int b = 0; b < 2; b++)
 			{
 				const int c = (nchunks - 1) - (((nchunks - 1) & 1) != b ? 1 : 0);
 				if(c >= 0)
 					mbar_wait_bounded(&bars[b], (c >> 1) & 1, a.status);
 			}
+			if(ftma)
+				mbar_wait_bounded(&fbar, 0, a.status);
+		}
 	}
 	F::flush(a, s, fsm, W, H, tx0, ty0);
 }

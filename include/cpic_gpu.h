@@ -206,6 +206,13 @@ CPIC_API int cpic_compact(cpic_ctx_t *ctx, int32_t slack_pct);
  * capacity slack in percent}. */
 CPIC_API int cpic_tile_info(const cpic_ctx_t *ctx, int32_t *out);
 
+/* How the fused particle kernel stages each tile's field: *mode = 1 when
+ * the mixed form copies it with one 2D tensor copy per tile (tiles of an
+ * even width up to 254 cells, an even nx; tiles in the grid's last column
+ * or row, whose nodes wrap, load by threads), 0 when every tile loads by
+ * threads (the FP64 form reads E from global memory). */
+CPIC_API int cpic_field_tile_copy(const cpic_ctx_t *ctx, int32_t *mode);
+
 /* Health of the tile layout, out[4]: {overflow records (particles that
  * found no room in their destination tile) seen at the last host check,
  * layout rebuilds forced by overflows so far, current capacity slack in

@@ -123,11 +123,27 @@ def test_mixed_field_energy(lib, nx, ny):
     m.close()
 
 
+def test_field_tile_copy_mode(lib):
+    """The mixed form stages field tiles with 2D tensor copies when tiles
+    have an even width; tiles of one cell, odd grids and the FP64 form
+    (E read from global memory) load by threads."""
+    even = cases.two_stream(nx=32, ny=32, n=32 * 32 * 2)
+    odd = grid_case(25, 15, ppc=2)
+    for case, precision, tile, want in ((even, _lib.MIXED, 16, 1), (even, _lib.MIXED, 2, 1),
+                                        (even, _lib.MIXED, 1, 0), (odd, _lib.MIXED, 0, 0),
+                                        (even, _lib.FP64, 16, 0)):
+        c = cases.make_gpu(case, precision=precision, tile=tile)
+        assert c.field_tile_copy() == want, (precision, tile)
+        c.close()
+
+
 @pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
 def test_tile_size_changes_nothing(lib, precision):
     """The same plasma with tiles of 1, 2, 4 and 16 cells: identical
     particles and fields (the deposit is exact integer arithmetic and the
-    gather reads the same E, so the tiling is invisible)."""
+    gather reads the same E, so the tiling is invisible; in the mixed form
+    the one-cell tiles load their field by threads, the others by 2D tensor
+    copies apart from the tiles of the grid's last column and row)."""
     case = cases.two_stream(nx=32, ny=32, n=32 * 32 * 8)
     runs = []
     for tile in (1, 2, 4, 16):
