@@ -127,6 +127,20 @@ def variants():
     return [("shipped", True), ("exact", True)]
 
 
+def _stale(stamp):
+    """Whether a file of this project that the build compiles or includes
+    (the shims, the oracle's FFT and generator headers, the harness, the
+    configuration parser) is newer than the stamp."""
+    deps = [os.path.join(HERE, "shims", f) for f in os.listdir(os.path.join(HERE, "shims"))]
+    deps += [os.path.join(HERE, f) for f in ("orc_fft.h", "seed_init.h", "ref_harness.c")]
+    deps += [os.path.join(HERE, "shims_portable", f)
+             for f in os.listdir(os.path.join(HERE, "shims_portable"))]
+    deps += [os.path.join(HERE, "exact", f) for f in os.listdir(os.path.join(HERE, "exact"))]
+    deps.append(os.path.join(ROOT, "cpic_gb300", "csrc", "cpic_conf.c"))
+    t = os.path.getmtime(stamp)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.isfile(d))
+
+
 def build(force=False):
     ref = ref_root()
     if ref is None:
@@ -135,7 +149,7 @@ def build(force=False):
     # one stamp per host architecture: the copy of this directory on the GPU
     # host carries the stamp of this one but none of its binaries
     stamp = os.path.join(OUT, "built_%s.txt" % platform.machine())
-    if os.path.exists(stamp) and not force:
+    if os.path.exists(stamp) and not force and not _stale(stamp):
         return OUT
     inc = ["-I", os.path.join(HERE, "shims"), "-I", os.path.join(ROOT, "include"),
            "-I", os.path.join(ref, "include")]

@@ -51,11 +51,10 @@ def test_max_over_ranks_gloo(tmp_path):
     assert [(tmp_path / ("rank%d" % k)).read_text() for k in (0, 1)] == ["2.0", "2.0"]
 
 
-def test_cpu_legs_skip_grids_not_power_of_two():
-    """On a grid whose side is not a power of two the oracle's transform is a
-    direct DFT (minutes per field solve at 1920^2): the reference arm prints
-    its unavailable line and the CPU baseline says why, both at once."""
-    import time
+def test_reference_arm_skips_grids_not_power_of_two():
+    """On a grid whose side is not a power of two the FFTW stand-in the
+    reference is built against here is far slower than FFTW: the reference
+    arm prints its unavailable line at once instead of a flattering time."""
     r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
                         "--warmup", "0", "--workload", "two_stream_1920"],
                        cwd=ROOT, capture_output=True, text=True, timeout=120,
@@ -63,9 +62,3 @@ def test_cpu_legs_skip_grids_not_power_of_two():
     assert r.returncode == 0, r.stderr[-2000:]
     out = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
     assert out["impl"] == "reference" and "not a power of two" in out["unavailable"]
-    sys.path.insert(0, ROOT)
-    import bench
-    t = time.perf_counter()
-    cb = bench.cpu_baseline(1920, 100, 0.2, 0.01, 0.01, 0.05, 1920 * 1920 * 100)
-    assert time.perf_counter() - t < 1.0
-    assert cb["value"] is None and "not a power of two" in cb["unavailable"]
