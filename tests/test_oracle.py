@@ -116,3 +116,20 @@ def test_cyclotron(orc):
     # the radius of a cyclotron orbit is v / |qB/m| = 10
     assert abs(np.mean(rad) - v) <= v * dt * dt
     assert np.max(np.abs(rad - np.mean(rad))) <= v * dt * dt
+
+
+def test_reference_build_goes_stale_with_its_inputs(tmp_path):
+    """The reference build is redone when a project file it compiles or
+    includes (here the oracle's FFT header) is newer than its stamp."""
+    import os
+    from oracle import build_ref
+    import time
+    stamp = tmp_path / "built.txt"
+    stamp.write_text("x")
+    later = time.time() + 86400
+    os.utime(stamp, (later, later))
+    assert not build_ref._stale(str(stamp))
+    header = os.path.join(os.path.dirname(build_ref.__file__), "orc_fft.h")
+    t = os.path.getmtime(header) - 10
+    os.utime(stamp, (t, t))
+    assert build_ref._stale(str(stamp))
